@@ -1,0 +1,361 @@
+"""Benchmark: 3D FP32 CPML FDTD, 256^3 cells, 2000 time steps (one "step" of this
+benchmark = one whole 2000-time-step simulation from zero fields).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the reference's 3D plain-FDTD configuration): 256^3 total cells at
+dx = 20 nm with a 12-cell CPML on all six faces, Courant 0.5, 32 seeded
+dielectric boxes (eps in [1, 12.11]) on eps = 2.085, an Ez point dipole at the
+centre driven by a 193 THz / 10 fs Gaussian pulse, 2000 steps.  Metric:
+Gcell-updates/s (one cell advanced one full step = one update).
+
+Prints one JSON line (rank 0).  Multi-GPU runs are independent replicas (the
+single-grid stepper does not shard); value = all ranks' updates / max time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIMS = (256, 256, 256)
+DX = 20e-9
+CPML = 12
+TSTEPS = 2000
+COURANT = 0.5
+# algorithmic bytes per cell-update of the fused stepper, float32:
+#   6 fields read + written (48 B) + Cb for Ex, Ey, Ez read (12 B) = 60 B,
+#   plus the CPML psi recursions: 4 psi arrays read + written (32 B) on the
+#   slab cells, 3 axes x 2 x 12 / 256 of the cells -> 9.0 B on average.
+B_INTERIOR = 60.0
+B_CPML_PER_SLAB_CELL = 32.0
+
+
+def b_alg(dims=DIMS, t=CPML):
+    frac = sum(2.0 * t / n for n in dims)
+    return B_INTERIOR + B_CPML_PER_SLAB_CELL * frac
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "fused3_256_cpml.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch")
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return out
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        loaded = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        out["sm_mhz"] = statistics.median(loaded) if loaded else None
+        out["sm_max_mhz"] = max(mx) if mx else None
+        out["reasons"] = sorted(reasons)
+        out["samples"] = len(rows)
+        return out
+
+
+def make_engine(eps, precision="fp32", dims=DIMS):
+    from prismo_gb300.engine import FDTDEngine
+    from prismo_gb300.grid import GridSpec, YeeGrid
+    from prismo_gb300.pml import PMLParams
+    from prismo_gb300.sources import GaussianPulse
+
+    grid = YeeGrid.from_total(dims, DX, CPML)
+    dt = grid.suggest_time_step(COURANT)
+    eng = FDTDEngine(grid.dimensions, grid.spacing, dt, is_2d=False, precision=precision,
+                     material_arrays={"eps_rel": eps}, pml=PMLParams(thickness=CPML))
+    wf = GaussianPulse(193e12, 10e-15)
+    c = tuple(n // 2 for n in dims)
+    idx = (np.array([c[0]]).reshape(1, 1, 1), np.array([c[1]]).reshape(1, 1, 1), np.array([c[2]]).reshape(1, 1, 1))
+    eng.add_source("Ez", eng.offsets("Ez", idx), None, wf)
+    times = np.cumsum(np.full(TSTEPS, dt))
+    amps = np.asarray(wf(times), dtype=np.float64).reshape(TSTEPS, 1)
+    return grid, eng, amps
+
+
+def reset(eng):
+    for s in eng.sets:
+        s.zero_()
+    for p in eng.psi:
+        p.zero_()
+    eng.lib.pc_set_current_set(eng.ctx, 0)
+
+
+def cpu_baseline_sample(dims=DIMS, nsteps=3):
+    """FP64 oracle stepper (corrected, CPML) on this host: a bounded sample."""
+    from oracle import fdtd64 as O
+    from prismo_gb300.workloads import boxes_3d
+
+    g = O.OracleGrid.from_total(*dims, DX, CPML)
+    dt = g.suggest_dt(COURANT)
+    eps = boxes_3d(dims, seed=0)
+    o = O.OracleFDTD(g, dt, {"eps_rel": eps}, cpml_layers=CPML)
+    o.F["Ez"][dims[0] // 2, dims[1] // 2, dims[2] // 2] = 1.0
+    o.step()  # warm-up (allocates psi)
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        o.step()
+    el = time.perf_counter() - t0
+    cells = dims[0] * dims[1] * dims[2]
+    return cells * nsteps / el / 1e9, el
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import fdtd64 as O
+    from prismo_gb300.workloads import boxes_3d
+
+    dims = DIMS
+    g = O.OracleGrid.from_total(*dims, DX, CPML)
+    dt = g.suggest_dt(COURANT)
+    eps = boxes_3d(dims, seed=0)
+    o = O.OracleFDTD(g, dt, {"eps_rel": eps}, cpml_layers=CPML)
+    wf = O.gaussian_pulse(193e12, 10e-15)
+    c = tuple(n // 2 for n in dims)
+    o.add_source("Ez", (np.array([[[c[0]]]]), np.array([[[c[1]]]]), np.array([[[c[2]]]])), wf)
+    per = 1  # time steps per bench step: a bounded sample of the 2000-step run
+    for _ in range(args.warmup):
+        o.run(per)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.run(per)
+    el = time.perf_counter() - t0
+    cells = float(np.prod(dims))
+    value = cells * per * args.steps / el / 1e9
+    line = {
+        "impl": "reference", "metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "3d_fp32_cpml_256: 256^3, dx=20nm, 12-cell CPML, 32 seeded boxes, Ez dipole, 2000 steps",
+                   "sample": f"{per} time step(s) of the 2000 per bench step", "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": "Gcell/s", "cores": 1, "kind": "port",
+                         "sample": f"{per} of 2000 time steps per bench step, NumPy float64 oracle, 1 thread"},
+        "e2e": {"value": value, "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--tsteps", type=int, default=TSTEPS, help="time steps per bench step")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+
+    from prismo_gb300.workloads import boxes_3d
+
+    eps = boxes_3d(DIMS, seed=0)
+    grid, eng, amps_full = make_engine(eps)
+    tsteps = args.tsteps
+    amps = amps_full[:tsteps]
+    cells = float(np.prod(DIMS))
+    stream = eng.stream
+
+    def one():
+        reset(eng)
+        eng.step(tsteps, amps)
+
+    for _ in range(max(args.warmup, 3)):
+        one()
+    eng.synchronize()
+    status = eng.check_status()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    n0 = eng.launch_count()
+    eng.profile(True)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        one()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ms_total = ev0.elapsed_time(ev1)
+    kern_ms, kern_n = eng.profile_read()
+    eng.profile(False)
+    launches = eng.launch_count() - n0
+    clk = clocks.stop()
+    status |= eng.check_status()
+    if ws > 1:
+        t = torch.tensor([ms_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    value = cells * tsteps * args.steps * ws / (ms_total / 1e3) / 1e9
+
+    # roofline of the dominant kernel (fused H+E stencil, one launch = one time step)
+    bpc = b_alg()
+    avg_launch_s = kern_ms / 1e3 / max(kern_n, 1)
+    achieved = bpc * cells / avg_launch_s / 1e9  # GB/s
+    peak, peak_kind = measured_peaks()
+    traffic = traffic_from_profile()
+
+    # end-to-end through the engine API with host buffers
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        e2e = run_e2e(eng, eps, amps, tsteps, cells)
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        v, el = cpu_baseline_sample(nsteps=3)
+        cpu = {"value": v, "unit": "Gcell/s", "cores": 1, "kind": "port",
+               "sample": f"3 time steps (of 2000) of the 256^3 CPML stepper, NumPy float64 oracle, {el:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "3d_fp32_cpml_256: 256^3 total cells, dx=20nm, 12-cell CPML, Courant 0.5, "
+                                   "32 seeded boxes eps U[1,12.11] on 2.085, Ez dipole 193THz/10fs",
+                       "time_steps_per_step": tsteps, "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "inputs larger than L2 (fields 2x403 MB)", "status": status},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "bytes_per_cell_update": bpc, "kernel": "fused3 (H+E+CPML)",
+                         "avg_launch_us": avg_launch_s * 1e6, "launches_timed": kern_n},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_e2e(eng, eps, amps, tsteps, cells, reps=2):
+    """Host inputs -> device -> simulate -> host outputs, per step."""
+    import torch
+
+    eps_h = torch.from_numpy(eps).pin_memory()
+    outs = [torch.empty(tuple(eng.component(c).shape), dtype=eng.dtype).pin_memory()
+            for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")]
+    stream = eng.stream
+    h2d = eps_h.numel() * eps_h.element_size()
+    d2h = sum(o.numel() * o.element_size() for o in outs)
+
+    def one():
+        eps_d = eps_h.to(eng.device, non_blocking=True)
+        eng._set_materials({"eps_rel": eps_d})
+        reset(eng)
+        eng.step(tsteps, amps)
+        for o, c in zip(outs, ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")):
+            o.copy_(eng.component(c), non_blocking=True)
+
+    one()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(reps):
+        one()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / reps
+    return {"value": cells * tsteps / (ms / 1e3) / 1e9, "unit": "Gcell/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": ms, "api": "prismo_gb300.engine.FDTDEngine (host eps in, host fields out)"}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,142 @@
+/*
+ * prismo_cuda.h -- C ABI of libprismo_cuda.so, the sm_103a FDTD engine behind
+ * Prismo's backend interface.
+ *
+ * The reference drives its time stepper from Python: `prismo.set_backend()`
+ * selects an array provider (backends/backend_manager.py:139-186) and
+ * `MaxwellUpdater.step` (core/solver.py:535-552) advances the Yee fields with
+ * array slicing.  A "cuda" backend binds these entry points through ctypes from
+ * Python; every pointer argument named `d_*` is a device
+ * pointer owned by the caller, every other pointer is host memory.
+ *
+ * Conventions
+ *   - Every call returns 0 (PC_OK) or a negative PC_ERR_* code.
+ *   - Field buffers use one padded layout for all six components:
+ *       3D: element (i, j, k) at ((i*ny + j) * pitch + k)
+ *       2D: element (i, j)    at (i * pitch + j)
+ *     with pitch >= the fast extent (nz in 3D, ny in 2D) and a multiple of 32.
+ *     Entries outside a component's own shape (core/grid.py:157-168) are zero
+ *     and stay zero.
+ *   - Component order is Ex, Ey, Ez, Hx, Hy, Hz (index 0..5).
+ *   - A context is not thread safe; separate contexts may run on separate
+ *     streams.  Device-side problems set bits in a status word (pc_status).
+ */
+#ifndef PRISMO_CUDA_H
+#define PRISMO_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PC_OK 0
+#define PC_ERR_INVALID (-1)      /* bad argument / unsupported combination */
+#define PC_ERR_CUDA (-2)         /* a CUDA runtime call failed */
+#define PC_ERR_TIMEOUT (-3)      /* a bounded device wait ran out */
+#define PC_ERR_NONFINITE (-4)    /* NaN/Inf detected in the fields */
+#define PC_ERR_STATE (-5)        /* call out of order (e.g. step before set_fields) */
+
+#define PC_STATUS_NONFINITE 0x1u
+#define PC_STATUS_TIMEOUT 0x2u
+#define PC_STATUS_BOUNDS 0x4u
+
+/* Stepper kinds */
+#define PC_MODE_CORRECTED 0 /* stable Yee scheme: H written to [...,1:-1,...] */
+#define PC_MODE_LEGACY 1    /* exact core/solver.py:167-456 semantics */
+
+/* Kernel schedule for the corrected 3D stepper */
+#define PC_SCHED_AUTO 0
+#define PC_SCHED_SPLIT 1 /* separate H and E passes, in place */
+#define PC_SCHED_FUSED 2 /* one fused H+E pass per step, ping-pong buffers */
+
+typedef struct pc_grid_desc {
+    int32_t ndim;      /* 2 or 3 */
+    int32_t nx, ny, nz; /* total Yee dimensions, core/grid.py:122-125 (nz = 1 in 2D) */
+    int32_t pitch;     /* elements per fast row of every field buffer */
+    int32_t precision; /* 4 = float32, 8 = float64 */
+    int32_t mode;      /* PC_MODE_* */
+    int32_t sched;     /* PC_SCHED_* */
+    double dt, dx, dy, dz;
+} pc_grid_desc;
+
+typedef struct pc_ctx pc_ctx;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int pc_version(void);
+
+/* Create / destroy a stepping context (replaces the state that
+ * MaxwellUpdater.__init__ builds, core/solver.py:42-79). */
+int pc_create(const pc_grid_desc* desc, pc_ctx** out);
+void pc_destroy(pc_ctx* ctx);
+
+/* Attach field storage: set0/set1 hold device pointers to the six components
+ * (Ex..Hz).  set1 may be NULL when the schedule does not ping-pong; the fused
+ * schedule writes step n+1 into the other set.  Replaces core/fields.py:64-70. */
+int pc_set_fields(pc_ctx* ctx, void* const set0[6], void* const set1[6]);
+
+/* Which set (0 or 1) currently holds the latest fields. */
+int pc_current_set(const pc_ctx* ctx);
+
+/* Declare which attached set holds the latest fields (e.g. after rebinding
+ * storage whose newest data sits in set 1). */
+int pc_set_current_set(pc_ctx* ctx, int32_t set);
+
+/* Build the interpolated update coefficients on the device from cell-centred
+ * material arrays (core/solver.py:113-133 and 458-533).  Inputs are float64
+ * device arrays of shape (nx, ny, nz), contiguous; any may be NULL (vacuum:
+ * eps_rel = mu_rel = 1, sigma = 0).  Outputs use the padded field layout in
+ * the context precision; d_ca / d_da / d_db outputs may be NULL to skip. */
+int pc_build_coefficients(pc_ctx* ctx, const double* d_eps_rel, const double* d_mu_rel,
+                          const double* d_sigma_e, const double* d_sigma_m, double eps0,
+                          double mu0, void* const d_ca[3], void* const d_cb[3],
+                          void* const d_da[3], void* const d_db[3], void* stream);
+
+/* Attach coefficients for E (Ca may be NULL: treated as 1) and H (arrays may be
+ * NULL: the scalars da, db are used for every H point). */
+int pc_set_coefficients(pc_ctx* ctx, const void* const d_ca[3], const void* const d_cb[3],
+                        const void* const d_da[3], const void* const d_db[3], double da,
+                        double db);
+
+/* Number of elements of one psi set for CPML thickness t (both slabs of all
+ * three axes, four components per axis). */
+size_t pc_cpml_psi_elems(const pc_grid_desc* desc, int32_t thickness);
+
+/* Enable the CPML: per-axis host arrays b, a, kappa of length nx, ny, nz
+ * (boundaries/pml.py:117-257 profiles; pass the z arrays as NULL in 2D), and
+ * one or two zeroed device psi sets of pc_cpml_psi_elems() elements. */
+int pc_set_cpml(pc_ctx* ctx, int32_t thickness, const double* const b[3], const double* const a[3],
+                const double* const kappa[3], void* d_psi0, void* d_psi1);
+
+/* Soft source: field[comp][offset[n]] += weight[n] * amplitude(t_{n+1}) after the
+ * E update of every step (sources/point.py:47-73, plane_wave.py:184-221).
+ * Offsets are element offsets in the padded layout.  Returns the source id
+ * (>= 0) or an error. */
+int pc_add_source(pc_ctx* ctx, int32_t comp, const int64_t* offsets, const double* weights,
+                  int32_t n);
+
+/* Advance nsteps leap-frog steps (H then E then sources), i.e. nsteps calls of
+ * MaxwellUpdater.step followed by Source.update_fields (core/simulation.py:147-164).
+ * amps: host array [nsteps][nsources] of source amplitudes (may be NULL when
+ * there are no sources). */
+int pc_step(pc_ctx* ctx, int32_t nsteps, const double* amps, void* stream);
+
+/* Read and clear the device status word (PC_STATUS_* bits). Synchronises the
+ * stream. */
+int pc_status(pc_ctx* ctx, uint32_t* flags, void* stream);
+
+/* Number of this library's kernels launched since the context was created. */
+int64_t pc_launch_count(const pc_ctx* ctx);
+
+/* Time the main stencil launch of every pc_step with a CUDA event pair on the
+ * launching stream (enable != 0), and read the summed milliseconds and the
+ * number of timed launches since the last read (synchronises the events). */
+int pc_profile(pc_ctx* ctx, int32_t enable);
+int pc_profile_read(pc_ctx* ctx, double* total_ms, int64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PRISMO_CUDA_H */

@@ -1,0 +1,24 @@
+"""GB300-native (sm_103a) FDTD time stepping behind Prismo's backend interface.
+
+The compute path is ``libprismo_cuda.so`` (hand-written CUDA, C ABI in
+include/prismo_cuda.h) driven through ctypes; PyTorch provides device memory
+and streams.  There is no CPU fallback: operations raise when the native
+library or a CUDA device is missing.
+"""
+
+__version__ = "0.1.0"
+
+from .grid import GridSpec, YeeGrid  # noqa: F401,E402
+from .pml import PMLParams  # noqa: F401,E402
+from .sources import (  # noqa: F401,E402
+    ContinuousWave,
+    CustomWaveform,
+    ElectricDipole,
+    GaussianPulse,
+    LineSource,
+    MagneticDipole,
+    PlaneWaveSource,
+    PointSource,
+    Source,
+    Waveform,
+)

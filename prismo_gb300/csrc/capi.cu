@@ -1,0 +1,304 @@
+// extern "C" entry points of libprismo_cuda.so (declared in include/prismo_cuda.h).
+#include <stdlib.h>
+#include <string.h>
+
+#include <new>
+#include <vector>
+
+#include "pc_internal.cuh"
+
+namespace pc {
+
+PsiLayout psi_layout(const pc_grid_desc& g, int t) {
+    PsiLayout L{};
+    L.t = t;
+    if (t <= 0) return L;
+    const int64_t T2 = 2 * (int64_t)t;
+    if (g.ndim == 3) {
+        L.slot_elems[0] = T2 * g.ny * g.pitch;
+        L.slot_elems[1] = (int64_t)g.nx * T2 * g.pitch;
+        L.slot_elems[2] = (int64_t)g.nx * g.ny * T2;
+    } else {
+        L.slot_elems[0] = T2 * g.pitch;
+        L.slot_elems[1] = (int64_t)g.nx * T2;
+        L.slot_elems[2] = 0;
+    }
+    int64_t off = 0;
+    for (int ax = 0; ax < 3; ++ax) {
+        L.axis_base[ax] = off;
+        off += 4 * L.slot_elems[ax];
+    }
+    L.total = off;
+    return L;
+}
+
+}  // namespace pc
+
+using namespace pc;
+
+static int validate(const pc_grid_desc* d) {
+    if (!d) return PC_ERR_INVALID;
+    if (d->ndim != 2 && d->ndim != 3) return PC_ERR_INVALID;
+    if (d->precision != 4 && d->precision != 8) return PC_ERR_INVALID;
+    if (d->mode != PC_MODE_CORRECTED && d->mode != PC_MODE_LEGACY) return PC_ERR_INVALID;
+    if (d->sched < PC_SCHED_AUTO || d->sched > PC_SCHED_FUSED) return PC_ERR_INVALID;
+    if (d->nx < 3 || d->ny < 3) return PC_ERR_INVALID;
+    if (d->ndim == 3 && d->nz < 3) return PC_ERR_INVALID;
+    if (d->ndim == 2 && d->nz != 1) return PC_ERR_INVALID;
+    const int fast = d->ndim == 3 ? d->nz : d->ny;
+    if (d->pitch < fast || (d->pitch % 32) != 0) return PC_ERR_INVALID;
+    if (!(d->dt > 0) || !(d->dx > 0) || !(d->dy > 0)) return PC_ERR_INVALID;
+    if (d->ndim == 3 && !(d->dz > 0)) return PC_ERR_INVALID;
+    if ((int64_t)d->nx * d->ny * d->pitch > ((int64_t)1 << 40)) return PC_ERR_INVALID;
+    return PC_OK;
+}
+
+extern "C" {
+
+int pc_version(void) { return 100; }
+
+int pc_create(const pc_grid_desc* desc, pc_ctx** out) {
+    if (!out) return PC_ERR_INVALID;
+    *out = nullptr;
+    int rc = validate(desc);
+    if (rc) return rc;
+    pc_ctx* c = new (std::nothrow) pc_ctx();
+    if (!c) return PC_ERR_INVALID;
+    c->g = *desc;
+    if (c->g.sched == PC_SCHED_AUTO)
+        c->g.sched = (c->g.ndim == 3 && c->g.mode == PC_MODE_CORRECTED) ? PC_SCHED_FUSED : PC_SCHED_SPLIT;
+    if (c->g.mode == PC_MODE_LEGACY || c->g.ndim == 2) c->g.sched = PC_SCHED_SPLIT;
+    c->da_s = 1.0;
+    c->db_s = 0.0;
+    if (cudaMalloc(&c->d_status, 2 * sizeof(uint32_t)) != cudaSuccess) {
+        delete c;
+        return PC_ERR_CUDA;
+    }
+    c->d_legacy_flags = c->d_status + 1;
+    if (cudaMemset(c->d_status, 0, 2 * sizeof(uint32_t)) != cudaSuccess) {
+        cudaFree(c->d_status);
+        delete c;
+        return PC_ERR_CUDA;
+    }
+    *out = c;
+    return PC_OK;
+}
+
+void pc_destroy(pc_ctx* c) {
+    if (!c) return;
+    for (auto& s : c->sources) {
+        cudaFree(s.d_off);
+        cudaFree(s.d_w);
+    }
+    cudaFree(c->d_amps);
+    cudaFree(c->d_cpml_coef);
+    cudaFree(c->d_status);
+    for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
+    destroy_fused_state(c);
+    delete c;
+}
+
+int pc_set_fields(pc_ctx* c, void* const set0[6], void* const set1[6]) {
+    if (!c || !set0) return PC_ERR_INVALID;
+    for (int q = 0; q < 6; ++q) {
+        if (!set0[q]) return PC_ERR_INVALID;
+        c->F[0][q] = set0[q];
+        c->F[1][q] = set1 ? set1[q] : nullptr;
+        if (set1 && !set1[q]) return PC_ERR_INVALID;
+    }
+    if (c->g.sched == PC_SCHED_FUSED && !set1) return PC_ERR_INVALID;
+    c->cur = 0;
+    c->have_fields = true;
+    return PC_OK;
+}
+
+int pc_current_set(const pc_ctx* c) { return c ? c->cur : PC_ERR_INVALID; }
+
+int pc_set_current_set(pc_ctx* c, int32_t set) {
+    if (!c || set < 0 || set > 1) return PC_ERR_INVALID;
+    if (set == 1 && !c->F[1][0]) return PC_ERR_INVALID;
+    c->cur = set;
+    return PC_OK;
+}
+
+int pc_build_coefficients(pc_ctx* c, const double* eps, const double* mu, const double* sig,
+                          const double* sigm, double eps0, double mu0, void* const ca[3],
+                          void* const cb[3], void* const da[3], void* const db[3], void* stream) {
+    if (!c || !(eps0 > 0) || !(mu0 > 0)) return PC_ERR_INVALID;
+    return launch_build_coefficients(c->g, eps, mu, sig, sigm, eps0, mu0, ca, cb, da, db,
+                                     (cudaStream_t)stream, &c->launches);
+}
+
+int pc_set_coefficients(pc_ctx* c, const void* const ca[3], const void* const cb[3],
+                        const void* const da[3], const void* const db[3], double da_s, double db_s) {
+    if (!c || !cb) return PC_ERR_INVALID;
+    for (int q = 0; q < 3; ++q) {
+        if (!cb[q]) return PC_ERR_INVALID;
+        c->cb[q] = cb[q];
+        c->ca[q] = ca ? ca[q] : nullptr;
+        c->da[q] = da ? da[q] : nullptr;
+        c->db[q] = db ? db[q] : nullptr;
+        if ((c->da[q] == nullptr) != (c->db[q] == nullptr)) return PC_ERR_INVALID;
+    }
+    c->da_s = da_s;
+    c->db_s = db_s;
+    c->have_coef = true;
+    return PC_OK;
+}
+
+size_t pc_cpml_psi_elems(const pc_grid_desc* d, int32_t t) {
+    if (validate(d) || t <= 0) return 0;
+    return (size_t)psi_layout(*d, t).total;
+}
+
+int pc_set_cpml(pc_ctx* c, int32_t t, const double* const b[3], const double* const a[3],
+                const double* const kappa[3], void* psi0, void* psi1) {
+    if (!c) return PC_ERR_INVALID;
+    if (t <= 0) {
+        c->cpml_t = 0;
+        return PC_OK;
+    }
+    if (c->g.mode == PC_MODE_LEGACY) return PC_ERR_INVALID;  // the reference has no CPML
+    const pc_grid_desc& g = c->g;
+    const int naxes = g.ndim;
+    const int n[3] = {g.nx, g.ny, g.ndim == 3 ? g.nz : 0};
+    for (int ax = 0; ax < naxes; ++ax) {
+        if (!b || !a || !kappa || !b[ax] || !a[ax] || !kappa[ax]) return PC_ERR_INVALID;
+        if (2 * t > n[ax]) return PC_ERR_INVALID;
+    }
+    if (!psi0) return PC_ERR_INVALID;
+    if (g.sched == PC_SCHED_FUSED && !psi1) return PC_ERR_INVALID;
+    const int64_t total = 3 * ((int64_t)n[0] + n[1] + n[2]);
+    const size_t es = (size_t)g.precision;
+    std::vector<unsigned char> host(total * es);
+    int64_t off = 0;
+    for (int ax = 0; ax < 3; ++ax) {
+        for (int w = 0; w < 3; ++w) {
+            for (int i = 0; i < n[ax]; ++i) {
+                double v = w == 0 ? b[ax][i] : (w == 1 ? a[ax][i] : 1.0 / kappa[ax][i]);
+                if (es == 8)
+                    ((double*)host.data())[off + i] = v;
+                else
+                    ((float*)host.data())[off + i] = (float)v;
+            }
+            off += n[ax];
+        }
+    }
+    cudaFree(c->d_cpml_coef);
+    c->d_cpml_coef = nullptr;
+    PC_CUDA_CHECK(cudaMalloc(&c->d_cpml_coef, host.size()));
+    PC_CUDA_CHECK(cudaMemcpy(c->d_cpml_coef, host.data(), host.size(), cudaMemcpyHostToDevice));
+    c->cpml_t = t;
+    c->psi[0] = psi0;
+    c->psi[1] = psi1;
+    return PC_OK;
+}
+
+int pc_add_source(pc_ctx* c, int32_t comp, const int64_t* offsets, const double* weights, int32_t n) {
+    if (!c || comp < 0 || comp > 5 || n <= 0 || !offsets) return PC_ERR_INVALID;
+    if ((int)c->sources.size() >= PC_MAX_SOURCES) return PC_ERR_INVALID;
+    const int64_t lim = (int64_t)c->g.nx * c->g.ny * c->g.pitch;
+    for (int i = 0; i < n; ++i)
+        if (offsets[i] < 0 || offsets[i] >= lim) return PC_ERR_INVALID;
+    SourceDesc d{};
+    d.comp = comp;
+    d.n = n;
+    PC_CUDA_CHECK(cudaMalloc(&d.d_off, n * sizeof(int64_t)));
+    if (cudaMalloc(&d.d_w, n * sizeof(double)) != cudaSuccess) {
+        cudaFree(d.d_off);
+        return PC_ERR_CUDA;
+    }
+    std::vector<double> w(n, 1.0);
+    if (weights) memcpy(w.data(), weights, n * sizeof(double));
+    if (cudaMemcpy(d.d_off, offsets, n * sizeof(int64_t), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(d.d_w, w.data(), n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(d.d_off);
+        cudaFree(d.d_w);
+        return PC_ERR_CUDA;
+    }
+    c->sources.push_back(d);
+    return (int)c->sources.size() - 1;
+}
+
+int pc_step(pc_ctx* c, int32_t nsteps, const double* amps, void* stream) {
+    if (!c || nsteps < 0) return PC_ERR_INVALID;
+    if (!c->have_fields || !c->have_coef) return PC_ERR_STATE;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t ns = c->sources.size();
+    if (ns > 0) {
+        if (!amps) return PC_ERR_INVALID;
+        const size_t need = (size_t)nsteps * ns;
+        if (need > c->amps_cap) {
+            PC_CUDA_CHECK(cudaStreamSynchronize(s));
+            cudaFree(c->d_amps);
+            c->d_amps = nullptr;
+            c->amps_cap = 0;
+            PC_CUDA_CHECK(cudaMalloc(&c->d_amps, need * sizeof(double)));
+            c->amps_cap = need;
+        }
+        if (need) PC_CUDA_CHECK(cudaMemcpyAsync(c->d_amps, amps, need * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    for (int n = 0; n < nsteps; ++n) {
+        int rc;
+        cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+        if (c->prof_on) {
+            if (c->prof_used + 2 > c->prof_ev.size()) {
+                for (int q = 0; q < 2; ++q) {
+                    cudaEvent_t e;
+                    PC_CUDA_CHECK(cudaEventCreate(&e));
+                    c->prof_ev.push_back(e);
+                }
+            }
+            ev0 = c->prof_ev[c->prof_used];
+            ev1 = c->prof_ev[c->prof_used + 1];
+            c->prof_used += 2;
+            PC_CUDA_CHECK(cudaEventRecord(ev0, s));
+        }
+        if (c->g.mode == PC_MODE_LEGACY)
+            rc = launch_legacy_step(c, s);
+        else if (c->g.sched == PC_SCHED_FUSED)
+            rc = launch_fused_step(c, s);
+        else
+            rc = launch_split_step(c, s);
+        if (rc) return rc;
+        if (ev1) PC_CUDA_CHECK(cudaEventRecord(ev1, s));
+        rc = launch_sources(c, n, s);
+        if (rc) return rc;
+    }
+    return PC_OK;
+}
+
+int pc_status(pc_ctx* c, uint32_t* flags, void* stream) {
+    if (!c || !flags) return PC_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    PC_CUDA_CHECK(cudaMemcpyAsync(flags, c->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    PC_CUDA_CHECK(cudaMemsetAsync(c->d_status, 0, sizeof(uint32_t), s));
+    PC_CUDA_CHECK(cudaStreamSynchronize(s));
+    return PC_OK;
+}
+
+int64_t pc_launch_count(const pc_ctx* c) { return c ? c->launches : -1; }
+
+int pc_profile(pc_ctx* c, int32_t enable) {
+    if (!c) return PC_ERR_INVALID;
+    c->prof_on = enable != 0;
+    c->prof_used = 0;
+    return PC_OK;
+}
+
+int pc_profile_read(pc_ctx* c, double* total_ms, int64_t* count) {
+    if (!c || !total_ms || !count) return PC_ERR_INVALID;
+    double tot = 0.0;
+    for (size_t q = 0; q + 1 < c->prof_used; q += 2) {
+        PC_CUDA_CHECK(cudaEventSynchronize(c->prof_ev[q + 1]));
+        float ms = 0.f;
+        PC_CUDA_CHECK(cudaEventElapsedTime(&ms, c->prof_ev[q], c->prof_ev[q + 1]));
+        tot += ms;
+    }
+    *total_ms = tot;
+    *count = (int64_t)(c->prof_used / 2);
+    c->prof_used = 0;
+    return PC_OK;
+}
+
+}  // extern "C"

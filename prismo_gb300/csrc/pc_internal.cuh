@@ -1,0 +1,122 @@
+// Internal declarations shared by the libprismo_cuda translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/prismo_cuda.h"
+
+#define PC_MAX_SOURCES 64
+
+namespace pc {
+
+// Psi slot numbering inside each axis block (four components per axis).
+//   x: Eyx Ezx Hyx Hzx   y: Exy Ezy Hxy Hzy   z: Exz Eyz Hxz Hyz
+enum { SX_EY = 0, SX_EZ = 1, SX_HY = 2, SX_HZ = 3 };
+enum { SY_EX = 0, SY_EZ = 1, SY_HX = 2, SY_HZ = 3 };
+enum { SZ_EX = 0, SZ_EY = 1, SZ_HX = 2, SZ_HY = 3 };
+
+struct SourceDesc {
+    int comp;
+    int n;
+    int64_t* d_off;   // device offsets
+    double* d_w;      // device weights (float64, converted in-kernel)
+};
+
+// Geometry of the slab-only psi storage.  Axis a keeps four slots; the lower
+// slab index s = idx (idx < t), the upper s = idx - (n - 2t) (idx >= n - t).
+struct PsiLayout {
+    int t;
+    int64_t slot_elems[3];  // elements per slot for axis x, y, z
+    int64_t axis_base[3];   // element offset of each axis block
+    int64_t total;
+};
+
+PsiLayout psi_layout(const pc_grid_desc& g, int t);
+
+template <typename T>
+struct CpmlArgs {
+    int t;
+    const T* b[3];     // recursion decay, length n_axis
+    const T* a[3];     // recursion gain, length n_axis
+    const T* kinv[3];  // 1/kappa, length n_axis
+    const T* psi_in;   // read set
+    T* psi_out;        // write set (== psi_in for in-place schedules)
+    int64_t slot_elems[3];
+    int64_t axis_base[3];
+};
+
+template <typename T>
+struct FieldArgs {
+    int nx, ny, nz, pitch;
+    T dx, dy, dz;            // spacings (legacy kernels divide, as numpy does)
+    T inv_dx, inv_dy, inv_dz;
+    const T* Ein[3];
+    const T* Hin[3];
+    T* Eout[3];
+    T* Hout[3];
+    const T* ca[3];  // nullable: Ca == 1
+    const T* cb[3];
+    const T* da[3];  // nullable: scalar da_s
+    const T* db[3];  // nullable: scalar db_s
+    T da_s, db_s;
+    uint32_t* status;
+};
+
+}  // namespace pc
+
+struct pc_ctx {
+    pc_grid_desc g;
+    void* F[2][6];
+    int cur;
+    bool have_fields;
+    bool have_coef;
+    const void* ca[3];
+    const void* cb[3];
+    const void* da[3];
+    const void* db[3];
+    double da_s, db_s;
+    // CPML
+    int cpml_t;
+    void* psi[2];
+    void* d_cpml_coef;  // [3 axes][b, a, kinv][n_axis] in context precision
+    // sources
+    std::vector<pc::SourceDesc> sources;
+    double* d_amps;
+    size_t amps_cap;
+    // fused schedule: cached tensor maps and the chosen x-chunk length
+    void* fused_state;
+    int fused_cx;
+    // optional CUDA-event timing of the main stencil launch of every step
+    bool prof_on;
+    std::vector<cudaEvent_t> prof_ev;  // start/stop pairs, recycled
+    size_t prof_used;
+    // status
+    uint32_t* d_status;
+    uint32_t* d_legacy_flags;
+    int64_t launches;
+};
+
+// ---- launchers (host functions, defined in the .cu files) -------------------
+namespace pc {
+
+int launch_build_coefficients(const pc_grid_desc& g, const double* eps, const double* mu,
+                              const double* sig, const double* sigm, double eps0, double mu0,
+                              void* const ca[3], void* const cb[3], void* const da[3],
+                              void* const db[3], cudaStream_t s, int64_t* launches);
+
+int launch_legacy_step(pc_ctx* c, cudaStream_t s);
+int launch_split_step(pc_ctx* c, cudaStream_t s);
+int launch_sources(pc_ctx* c, int step_in_batch, cudaStream_t s);
+int launch_fused_step(pc_ctx* c, cudaStream_t s);
+void destroy_fused_state(pc_ctx* c);
+
+}  // namespace pc
+
+#define PC_CUDA_CHECK(x)                          \
+    do {                                          \
+        cudaError_t err__ = (x);                  \
+        if (err__ != cudaSuccess) return PC_ERR_CUDA; \
+    } while (0)

@@ -1,0 +1,122 @@
+// Device helpers shared by the corrected-stepper kernels.
+#pragma once
+
+#include "pc_internal.cuh"
+
+namespace pc {
+
+struct Idx3 {
+    int i, j, k, nx, ny, nz, pitch;
+};
+struct Idx2 {
+    int i, j, nx, ny, pitch;
+};
+
+template <typename T>
+__device__ __forceinline__ T hcoef(const T* p, int64_t o, T s) {
+    return p ? p[o] : s;
+}
+template <typename T>
+__device__ __forceinline__ T ecoef(const T* p, int64_t o) {
+    return p ? p[o] : T(1);
+}
+
+// Slab index of idx along an axis of length n with thickness t, or -1.
+__device__ __forceinline__ int slab_of(int idx, int n, int t) {
+    return idx < t ? idx : (idx >= n - t ? idx - (n - 2 * t) : -1);
+}
+
+// CPML-modified derivative for a 3D point: returns kinv*d + psi after
+// psi <- b psi + a d.  AX selects the derivative axis (0=x, 1=y, 2=z).
+template <typename T, int AX>
+__device__ __forceinline__ T cpml3(const CpmlArgs<T>& p, int slot, const Idx3& q, T d) {
+    const int idx = AX == 0 ? q.i : (AX == 1 ? q.j : q.k);
+    const int n = AX == 0 ? q.nx : (AX == 1 ? q.ny : q.nz);
+    const int s = slab_of(idx, n, p.t);
+    if (s < 0) return d;
+    int64_t po;
+    if (AX == 0)
+        po = ((int64_t)s * q.ny + q.j) * q.pitch + q.k;
+    else if (AX == 1)
+        po = ((int64_t)q.i * (2 * p.t) + s) * q.pitch + q.k;
+    else
+        po = ((int64_t)q.i * q.ny + q.j) * (2 * p.t) + s;
+    po += p.axis_base[AX] + (int64_t)slot * p.slot_elems[AX];
+    const T psi = p.b[AX][idx] * p.psi_in[po] + p.a[AX][idx] * d;
+    p.psi_out[po] = psi;
+    return d * p.kinv[AX][idx] + psi;
+}
+
+template <typename T, int AX>
+__device__ __forceinline__ T cpml2(const CpmlArgs<T>& p, int slot, const Idx2& q, T d) {
+    const int idx = AX == 0 ? q.i : q.j;
+    const int n = AX == 0 ? q.nx : q.ny;
+    const int s = slab_of(idx, n, p.t);
+    if (s < 0) return d;
+    int64_t po;
+    if (AX == 0)
+        po = (int64_t)s * q.pitch + q.j;
+    else
+        po = (int64_t)q.i * (2 * p.t) + s;
+    po += p.axis_base[AX] + (int64_t)slot * p.slot_elems[AX];
+    const T psi = p.b[AX][idx] * p.psi_in[po] + p.a[AX][idx] * d;
+    p.psi_out[po] = psi;
+    return d * p.kinv[AX][idx] + psi;
+}
+
+template <typename T>
+static FieldArgs<T> make_field_args(pc_ctx* c, int in_set, int out_set) {
+    FieldArgs<T> a{};
+    const pc_grid_desc& g = c->g;
+    a.nx = g.nx;
+    a.ny = g.ny;
+    a.nz = g.nz;
+    a.pitch = g.pitch;
+    a.dx = T(g.dx);
+    a.dy = T(g.dy);
+    a.dz = T(g.dz);
+    a.inv_dx = T(1.0 / g.dx);
+    a.inv_dy = T(1.0 / g.dy);
+    a.inv_dz = g.ndim == 3 ? T(1.0 / g.dz) : T(0);
+    for (int q = 0; q < 3; ++q) {
+        a.Ein[q] = static_cast<const T*>(c->F[in_set][q]);
+        a.Hin[q] = static_cast<const T*>(c->F[in_set][3 + q]);
+        a.Eout[q] = static_cast<T*>(c->F[out_set][q]);
+        a.Hout[q] = static_cast<T*>(c->F[out_set][3 + q]);
+        a.ca[q] = static_cast<const T*>(c->ca[q]);
+        a.cb[q] = static_cast<const T*>(c->cb[q]);
+        a.da[q] = static_cast<const T*>(c->da[q]);
+        a.db[q] = static_cast<const T*>(c->db[q]);
+    }
+    a.da_s = T(c->da_s);
+    a.db_s = T(c->db_s);
+    a.status = c->d_status;
+    return a;
+}
+
+template <typename T>
+static CpmlArgs<T> make_cpml_args(pc_ctx* c, int in_set, int out_set) {
+    CpmlArgs<T> p{};
+    p.t = c->cpml_t;
+    if (p.t <= 0) return p;
+    const pc_grid_desc& g = c->g;
+    const int n[3] = {g.nx, g.ny, g.ndim == 3 ? g.nz : 0};
+    const T* base = static_cast<const T*>(c->d_cpml_coef);
+    int64_t off = 0;
+    for (int ax = 0; ax < 3; ++ax) {
+        p.b[ax] = base + off;
+        p.a[ax] = base + off + n[ax];
+        p.kinv[ax] = base + off + 2 * n[ax];
+        off += 3 * (int64_t)n[ax];
+    }
+    PsiLayout L = psi_layout(g, p.t);
+    for (int ax = 0; ax < 3; ++ax) {
+        p.slot_elems[ax] = L.slot_elems[ax];
+        p.axis_base[ax] = L.axis_base[ax];
+    }
+    p.psi_in = static_cast<const T*>(c->psi[in_set] ? c->psi[in_set] : c->psi[0]);
+    p.psi_out = static_cast<T*>(c->psi[out_set] ? c->psi[out_set] : c->psi[0]);
+    return p;
+}
+
+}  // namespace pc

@@ -1,0 +1,277 @@
+"""Device-side FDTD engine: one libprismo_cuda context plus its device buffers.
+
+Field storage (one allocation per set): a tensor of shape (6, nx, ny, pitch) in
+3D or (6, nx, pitch) in 2D, component order Ex, Ey, Ez, Hx, Hy, Hz, fast axis
+padded to a multiple of 32 elements (128 B rows in float32).  Each component's
+reference-shaped array (core/grid.py:157-168) is a strided view of its slab;
+the padding stays zero.  The fused 3D schedule alternates between two such
+sets (reads set ``cur``, writes ``cur ^ 1``); the split schedule updates one
+set in place.
+
+Coefficients are built on the device from cell-centred material arrays
+(core/solver.py:113-133, 458-533) and kept in the same padded layout: Cb per E
+component always, Ca only when some sigma_e != 0, Da/Db arrays only when
+mu_rel != 1 or sigma_m != 0 (otherwise the scalars 1 and dt/mu0).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .pml import PMLParams, cpml_axis_coefficients
+
+EPS0 = 8.854187817e-12
+MU0 = 4 * np.pi * 1e-7
+COMPONENTS = ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")
+COMP_INDEX = {c: i for i, c in enumerate(COMPONENTS)}
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def component_shape(comp: str, dims, is_2d: bool):
+    """core/grid.py:157-168."""
+    nx, ny, nz = dims
+    if is_2d:
+        return {"Ex": (nx, ny - 1), "Ey": (nx - 1, ny), "Ez": (nx - 1, ny - 1),
+                "Hx": (nx - 1, ny), "Hy": (nx, ny - 1), "Hz": (nx, ny)}[comp]
+    return {"Ex": (nx, ny - 1, nz - 1), "Ey": (nx - 1, ny, nz - 1), "Ez": (nx - 1, ny - 1, nz),
+            "Hx": (nx - 1, ny, nz), "Hy": (nx, ny - 1, nz), "Hz": (nx, ny, nz - 1)}[comp]
+
+
+def _round_up(x: int, m: int) -> int:
+    return (x + m - 1) // m * m
+
+
+class FDTDEngine:
+    """Owns a native stepping context; see module docstring for the layout."""
+
+    def __init__(self, dims: Sequence[int], spacing: Sequence[float], dt: float, *, is_2d: bool,
+                 precision: str = "fp32", mode: str = "corrected", sched: str = "auto",
+                 material_arrays: Optional[dict] = None, pml: Optional[PMLParams] = None,
+                 device: str = "cuda:0", stream=None):
+        torch = _torch()
+        self.lib = _lib.load()
+        if not torch.cuda.is_available():
+            raise RuntimeError("the cuda backend needs a CUDA device")
+        self.device = torch.device(device)
+        self.is_2d = bool(is_2d)
+        nx, ny, nz = (int(d) for d in dims)
+        if self.is_2d:
+            nz = 1
+        self.dims = (nx, ny, nz)
+        self.spacing = tuple(float(s) for s in spacing)
+        self.dt = float(dt)
+        if precision not in ("fp32", "fp64"):
+            raise ValueError("precision must be 'fp32' or 'fp64'")
+        self.precision = precision
+        self.dtype = torch.float32 if precision == "fp32" else torch.float64
+        self.mode = {"corrected": _lib.PC_MODE_CORRECTED, "legacy": _lib.PC_MODE_LEGACY}[mode]
+        self.sched = {"auto": _lib.PC_SCHED_AUTO, "split": _lib.PC_SCHED_SPLIT,
+                      "fused": _lib.PC_SCHED_FUSED}[sched]
+        fast = ny if self.is_2d else nz
+        self.pitch = _round_up(fast, 32)
+        self.buf_shape = (6, nx, self.pitch) if self.is_2d else (6, nx, ny, self.pitch)
+        self.stream = stream if stream is not None else torch.cuda.current_stream(self.device)
+
+        desc = _lib.GridDesc()
+        desc.ndim = 2 if self.is_2d else 3
+        desc.nx, desc.ny, desc.nz = nx, ny, nz
+        desc.pitch = self.pitch
+        desc.precision = 4 if precision == "fp32" else 8
+        desc.mode = self.mode
+        desc.sched = self.sched
+        desc.dt = self.dt
+        desc.dx, desc.dy = self.spacing[0], self.spacing[1]
+        desc.dz = self.spacing[2] if not self.is_2d else 0.0
+        self.desc = desc
+        ctx = C.c_void_p()
+        _lib.check(self.lib.pc_create(C.byref(desc), C.byref(ctx)), "pc_create")
+        self.ctx = ctx
+        # the library resolves AUTO; ping-pong sets are needed for the fused 3D schedule
+        self.pingpong = (not self.is_2d) and self.mode == _lib.PC_MODE_CORRECTED and \
+            self.sched in (_lib.PC_SCHED_AUTO, _lib.PC_SCHED_FUSED)
+        with torch.cuda.device(self.device):
+            self.sets = [torch.zeros(self.buf_shape, dtype=self.dtype, device=self.device)]
+            if self.pingpong:
+                self.sets.append(torch.zeros(self.buf_shape, dtype=self.dtype, device=self.device))
+        s0 = _lib.P6(*[self.sets[0][q].data_ptr() for q in range(6)])
+        s1 = _lib.P6(*[self.sets[1][q].data_ptr() for q in range(6)]) if self.pingpong else None
+        _lib.check(self.lib.pc_set_fields(self.ctx, s0, s1), "pc_set_fields")
+        self._set_materials(material_arrays)
+        self.pml = None
+        self.psi = []
+        if pml is not None and int(pml.thickness) > 0:
+            self._set_cpml(pml)
+        self.sources = []  # (comp, offsets, weights, waveform)
+        self._closed = False
+
+    # -- setup ---------------------------------------------------------------
+    def _set_materials(self, ma: Optional[dict]):
+        torch = _torch()
+        ma = ma or {}
+        nx, ny, nz = self.dims
+        cell_shape = (nx, ny, nz)
+
+        def dev(name):
+            v = ma.get(name)
+            if v is None:
+                return None
+            if isinstance(v, torch.Tensor):
+                t = v.to(device=self.device, dtype=torch.float64).contiguous()
+            else:
+                t = torch.as_tensor(np.ascontiguousarray(np.asarray(v, dtype=np.float64)), device=self.device)
+            if tuple(t.shape) != cell_shape:
+                raise ValueError(f"{name} must have shape {cell_shape}, got {tuple(t.shape)}")
+            return t
+
+        eps, mu, sig, sigm = dev("eps_rel"), dev("mu_rel"), dev("sigma_e"), dev("sigma_m")
+        need_ca = sig is not None and bool(torch.any(sig != 0).item())
+        need_h = (mu is not None and bool(torch.any(mu != 1).item())) or \
+                 (sigm is not None and bool(torch.any(sigm != 0).item()))
+        ncoef = 3 + (3 if need_ca else 0) + (6 if need_h else 0)
+        shape = (ncoef,) + self.buf_shape[1:]
+        self.coef = torch.empty(shape, dtype=self.dtype, device=self.device)
+        cb = [self.coef[q] for q in range(3)]
+        ca = [self.coef[3 + q] for q in range(3)] if need_ca else [None] * 3
+        base = 3 + (3 if need_ca else 0)
+        da = [self.coef[base + q] for q in range(3)] if need_h else [None] * 3
+        db = [self.coef[base + 3 + q] for q in range(3)] if need_h else [None] * 3
+        sp = self._stream_ptr()
+        ptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        _lib.check(self.lib.pc_build_coefficients(
+            self.ctx, ptr(eps), ptr(mu), ptr(sig), ptr(sigm), EPS0, MU0,
+            _lib.ptr3(ca) if need_ca else None, _lib.ptr3(cb),
+            _lib.ptr3(da) if need_h else None, _lib.ptr3(db) if need_h else None, sp),
+            "pc_build_coefficients")
+        # scalar H coefficients for mu_rel = 1, sigma_m = 0 (core/solver.py:129-131)
+        db_s = (self.dt / (MU0 * 1.0)) / (1.0 + 0.0)
+        _lib.check(self.lib.pc_set_coefficients(
+            self.ctx, _lib.ptr3(ca) if need_ca else None, _lib.ptr3(cb),
+            _lib.ptr3(da) if need_h else None, _lib.ptr3(db) if need_h else None, 1.0, db_s),
+            "pc_set_coefficients")
+        self.has_ca, self.has_hcoef = need_ca, need_h
+        self._mat_refs = (eps, mu, sig, sigm)  # keep alive until the build kernel ran
+        self.synchronize()
+        self._mat_refs = None
+
+    def _set_cpml(self, params: PMLParams):
+        torch = _torch()
+        t = int(params.thickness)
+        nx, ny, nz = self.dims
+        d_max = max(self.spacing[:2] if self.is_2d else self.spacing)
+        ns = [nx, ny] + ([] if self.is_2d else [nz])
+        prof = [cpml_axis_coefficients(n, params, d_max, self.dt) for n in ns]
+        self._cpml_host = prof  # keep the float64 arrays alive during the call
+        arrs = [[np.ascontiguousarray(p[w]) for p in prof] for w in range(3)]
+        D = C.POINTER(C.c_double)
+        mk = lambda lst: _lib.D3(*([x.ctypes.data_as(D) for x in lst] + [None] * (3 - len(lst))))  # noqa: E731
+        nel = int(self.lib.pc_cpml_psi_elems(C.byref(self.desc), t))
+        self.psi = [torch.zeros(nel, dtype=self.dtype, device=self.device)]
+        if self.pingpong:
+            self.psi.append(torch.zeros(nel, dtype=self.dtype, device=self.device))
+        _lib.check(self.lib.pc_set_cpml(self.ctx, t, mk(arrs[0]), mk(arrs[1]), mk(arrs[2]),
+                                        self.psi[0].data_ptr(),
+                                        self.psi[1].data_ptr() if self.pingpong else None), "pc_set_cpml")
+        self.pml = params
+
+    # -- access --------------------------------------------------------------
+    def _stream_ptr(self):
+        return self.stream.cuda_stream
+
+    @property
+    def cur(self) -> int:
+        return int(self.lib.pc_current_set(self.ctx))
+
+    def component(self, comp: str, set_index: Optional[int] = None):
+        """Reference-shaped view (core/grid.py:157-168) of a component."""
+        q = COMP_INDEX[comp]
+        s = self.sets[self.cur if set_index is None else set_index]
+        shp = component_shape(comp, self.dims, self.is_2d)
+        if self.is_2d:
+            return s[q, : shp[0], : shp[1]]
+        return s[q, : shp[0], : shp[1], : shp[2]]
+
+    def offsets(self, comp: str, index) -> np.ndarray:
+        """Flat element offsets (padded layout) of a reference index tuple."""
+        shp = component_shape(comp, self.dims, self.is_2d)
+        grid = np.zeros(shp, dtype=bool)
+        grid[index] = True
+        idx = np.nonzero(grid)
+        if self.is_2d:
+            return (idx[0].astype(np.int64) * self.pitch + idx[1]).astype(np.int64)
+        ny = self.dims[1]
+        return ((idx[0].astype(np.int64) * ny + idx[1]) * self.pitch + idx[2]).astype(np.int64)
+
+    # -- sources ---------------------------------------------------------------
+    def add_source(self, comp: str, offsets: np.ndarray, weights: Optional[np.ndarray], waveform) -> int:
+        offs = np.ascontiguousarray(offsets, dtype=np.int64)
+        w = None if weights is None else np.ascontiguousarray(np.broadcast_to(weights, offs.shape), dtype=np.float64)
+        sid = _lib.check(self.lib.pc_add_source(
+            self.ctx, COMP_INDEX[comp], offs.ctypes.data_as(C.POINTER(C.c_int64)),
+            None if w is None else w.ctypes.data_as(C.POINTER(C.c_double)), int(offs.size)), "pc_add_source")
+        self.sources.append((comp, offs, w, waveform))
+        return sid
+
+    # -- stepping --------------------------------------------------------------
+    def step(self, nsteps: int = 1, amps: Optional[np.ndarray] = None):
+        """Advance nsteps; amps[nsteps, nsources] are the source amplitudes at
+        t_{n+1} of each step (sources/point.py:62-73)."""
+        ns = len(self.sources)
+        ap = None
+        if ns:
+            a = np.ascontiguousarray(amps, dtype=np.float64).reshape(nsteps, ns)
+            self._amps_keep = a
+            ap = a.ctypes.data_as(C.POINTER(C.c_double))
+        _lib.check(self.lib.pc_step(self.ctx, int(nsteps), ap, self._stream_ptr()), "pc_step")
+
+    def status(self) -> int:
+        v = C.c_uint32(0)
+        _lib.check(self.lib.pc_status(self.ctx, C.byref(v), self._stream_ptr()), "pc_status")
+        return int(v.value)
+
+    def check_status(self):
+        st = self.status()
+        if st & _lib.PC_STATUS_TIMEOUT:
+            raise TimeoutError("a bounded device wait ran out inside the FDTD kernel")
+        if st & _lib.PC_STATUS_NONFINITE:
+            raise FloatingPointError("non-finite field values detected")
+        return st
+
+    def profile(self, enable: bool = True):
+        _lib.check(self.lib.pc_profile(self.ctx, 1 if enable else 0), "pc_profile")
+
+    def profile_read(self):
+        """(summed ms, launches) of the main stencil kernel since the last read."""
+        ms = C.c_double(0)
+        n = C.c_int64(0)
+        _lib.check(self.lib.pc_profile_read(self.ctx, C.byref(ms), C.byref(n)), "pc_profile_read")
+        return float(ms.value), int(n.value)
+
+    def launch_count(self) -> int:
+        return int(self.lib.pc_launch_count(self.ctx))
+
+    def synchronize(self):
+        self.stream.synchronize()
+
+    def close(self):
+        if not self._closed and self.ctx:
+            try:
+                self.synchronize()
+            finally:
+                self.lib.pc_destroy(self.ctx)
+                self.ctx = C.c_void_p()
+                self._closed = True
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

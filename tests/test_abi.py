@@ -1,0 +1,75 @@
+"""CPU checks of the C ABI: the library builds, loads and exports every symbol
+that include/prismo_cuda.h declares (no compute calls: there is no GPU here)."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", f)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names |= set(re.findall(r"\b(pc_\w+)\s*\(", src))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from prismo_gb300 import _lib, build
+
+    if not os.path.exists(_lib.LIB_PATH):
+        build.build()
+    return _lib.load()
+
+
+def test_header_declares_api():
+    names = declared_symbols()
+    assert {"pc_create", "pc_step", "pc_destroy", "pc_set_fields", "pc_status"} <= names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_bindings_cover_header(lib):
+    from prismo_gb300 import _lib
+
+    assert declared_symbols() == set(_lib.SIGNATURES)
+
+
+def test_version_and_invalid_args_without_gpu(lib):
+    assert lib.pc_version() >= 100
+    from prismo_gb300 import _lib
+
+    d = _lib.GridDesc()
+    d.ndim = 4  # invalid -> rejected before any CUDA call
+    out = ctypes.c_void_p()
+    assert lib.pc_create(ctypes.byref(d), ctypes.byref(out)) == _lib.PC_ERR_INVALID
+    assert lib.pc_cpml_psi_elems(ctypes.byref(d), 4) == 0
+    d.ndim, d.nx, d.ny, d.nz, d.pitch, d.precision = 3, 16, 16, 16, 32, 4
+    d.mode, d.sched, d.dt, d.dx, d.dy, d.dz = 0, 0, 1e-17, 2e-8, 2e-8, 2e-8
+    # two slabs of 3 per axis, four slots per axis
+    want = 4 * (6 * 16 * 32) + 4 * (16 * 6 * 32) + 4 * (16 * 16 * 6)
+    assert lib.pc_cpml_psi_elems(ctypes.byref(d), 3) == want
+    d.pitch = 20  # not a multiple of 32
+    assert lib.pc_cpml_psi_elems(ctypes.byref(d), 3) == 0
+
+
+def test_error_mapping():
+    from prismo_gb300 import _lib
+
+    with pytest.raises(ValueError):
+        _lib.check(_lib.PC_ERR_INVALID, "x")
+    with pytest.raises(TimeoutError):
+        _lib.check(_lib.PC_ERR_TIMEOUT, "x")
+    with pytest.raises(FloatingPointError):
+        _lib.check(_lib.PC_ERR_NONFINITE, "x")
+    assert _lib.check(3) == 3

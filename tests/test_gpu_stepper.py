@@ -1,0 +1,184 @@
+"""GPU parity of the stepping kernels against the reference fixtures and the oracle.
+
+Tolerances: float64 kernels of the reference stepper must equal the reference
+bit for bit; float64 corrected kernels must match the FP64 oracle to 1e-12
+(relative to the field maximum); float32 kernels must match to relative L2
+<= 1e-5 per component.
+"""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import fdtd64 as O
+
+pytestmark = pytest.mark.gpu
+
+COMPS = O.COMPONENTS
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def make_engine(dims, spacing, dt, is_2d, **kw):
+    from prismo_gb300.engine import FDTDEngine
+
+    return FDTDEngine(dims, spacing, dt, is_2d=is_2d, **kw)
+
+
+def load_fields(eng, init, torch):
+    for c in COMPS:
+        eng.component(c).copy_(torch.from_numpy(np.asarray(init[c])).to(eng.device, eng.dtype))
+
+
+def read_fields(eng):
+    return {c: eng.component(c).double().cpu().numpy() for c in COMPS}
+
+
+def rel_l2(a, b):
+    n = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (n if n > 0 else 1.0)
+
+
+@pytest.mark.parametrize("name", ["ref_l0_3d.npz", "ref_l0_2d.npz"])
+def test_reference_stepper_fp64_is_bit_exact(torch, golden_dir, name):
+    z = np.load(os.path.join(golden_dir, name))
+    meta = json.loads(str(z["meta"]))
+    g = O.OracleGrid(tuple(meta["size"]), meta["resolution"], meta["layers"])
+    mats = {k: z[k] for k in ("eps_rel", "mu_rel", "sigma_e", "sigma_m")}
+    eng = make_engine(g.dims, g.spacing, meta["dt"], g.is_2d, precision="fp64", mode="legacy",
+                      material_arrays=mats)
+    load_fields(eng, {c: z[f"init_{c}"] for c in COMPS}, torch)
+    eng.step(meta["nsteps"])
+    out = read_fields(eng)
+    for c in COMPS:
+        np.testing.assert_array_equal(out[c], z[f"out_{c}"], err_msg=c)
+    eng.close()
+
+
+def _random_case(dims, is_2d, seed, lossy):
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = dims
+    d = 20e-9
+    if is_2d:
+        g = O.OracleGrid.from_total(nx, ny, 1, d, 3)
+    else:
+        g = O.OracleGrid.from_total(nx, ny, nz, d, 3)
+    mats = {"eps_rel": rng.uniform(1.0, 12.0, size=g.dims)}
+    if lossy:
+        mats["sigma_e"] = rng.uniform(0.0, 3e4, size=g.dims)
+        mats["mu_rel"] = rng.uniform(1.0, 1.5, size=g.dims)
+        mats["sigma_m"] = rng.uniform(0.0, 3e3, size=g.dims)
+    init = {}
+    for c in COMPS:
+        init[c] = rng.standard_normal(g.shape(c)) * (1.0 if c[0] == "E" else 1 / 377.0)
+    # respect the stepper invariants: boundary H entries that are never updated
+    return g, mats, init
+
+
+@pytest.mark.parametrize("sched", ["split", "fused"])
+@pytest.mark.parametrize("lossy", [False, True])
+@pytest.mark.parametrize("cpml", [0, 4])
+def test_corrected_3d_matches_oracle(torch, sched, lossy, cpml):
+    g, mats, init = _random_case((37, 29, 45), False, seed=11 + cpml + lossy, lossy=lossy)
+    dt = g.suggest_dt(0.5)
+    o = O.OracleFDTD(g, dt, mats, cpml_layers=cpml)
+    for c in COMPS:
+        o.F[c][...] = init[c]
+    nsteps = 20
+    o.run(nsteps)
+    from prismo_gb300.pml import PMLParams
+
+    pml = PMLParams(thickness=cpml) if cpml else None
+    for prec in ("fp64", "fp32"):
+        eng = make_engine(g.dims, g.spacing, dt, False, precision=prec, sched=sched, material_arrays=mats, pml=pml)
+        load_fields(eng, init, torch)
+        eng.step(nsteps)
+        out = read_fields(eng)
+        assert eng.check_status() == 0
+        for c in COMPS:
+            ref = o.F[c]
+            if prec == "fp64":
+                np.testing.assert_allclose(out[c], ref, rtol=0, atol=1e-12 * np.abs(ref).max(), err_msg=c)
+            else:
+                assert rel_l2(out[c], ref) <= 1e-5, (c, rel_l2(out[c], ref))
+        eng.close()
+
+
+@pytest.mark.parametrize("lossy", [False, True])
+@pytest.mark.parametrize("cpml", [0, 5])
+def test_corrected_2d_matches_oracle(torch, lossy, cpml):
+    g, mats, init = _random_case((53, 41, 1), True, seed=21 + cpml + lossy, lossy=lossy)
+    dt = g.suggest_dt(0.5)
+    o = O.OracleFDTD(g, dt, mats, cpml_layers=cpml)
+    for c in COMPS:
+        o.F[c][...] = init[c]
+    nsteps = 30
+    o.run(nsteps)
+    from prismo_gb300.pml import PMLParams
+
+    pml = PMLParams(thickness=cpml) if cpml else None
+    for prec in ("fp64", "fp32"):
+        eng = make_engine(g.dims, g.spacing, dt, True, precision=prec, material_arrays=mats, pml=pml)
+        load_fields(eng, init, torch)
+        eng.step(nsteps)
+        out = read_fields(eng)
+        for c in COMPS:
+            ref = o.F[c]
+            if prec == "fp64":
+                np.testing.assert_allclose(out[c], ref, rtol=0, atol=1e-12 * np.abs(ref).max(), err_msg=c)
+            else:
+                assert rel_l2(out[c], ref) <= 1e-5, (c, rel_l2(out[c], ref))
+        eng.close()
+
+
+def test_fused_equals_split_fp32_long_run(torch):
+    """The fused and split schedules implement the same arithmetic."""
+    g, mats, init = _random_case((70, 66, 100), False, seed=5, lossy=False)
+    dt = g.suggest_dt(0.5)
+    from prismo_gb300.pml import PMLParams
+
+    outs = []
+    for sched in ("split", "fused"):
+        eng = make_engine(g.dims, g.spacing, dt, False, precision="fp32", sched=sched, material_arrays=mats,
+                          pml=PMLParams(thickness=6))
+        load_fields(eng, init, torch)
+        eng.step(101)
+        outs.append(read_fields(eng))
+        eng.close()
+    for c in COMPS:
+        assert rel_l2(outs[1][c], outs[0][c]) <= 1e-6, c
+
+
+def test_point_source_matches_oracle(torch):
+    g = O.OracleGrid.from_total(31, 27, 25, 20e-9, 4)
+    dt = g.suggest_dt(0.5)
+    rng = np.random.default_rng(3)
+    mats = {"eps_rel": rng.uniform(1.0, 4.0, size=g.dims)}
+    wf = O.gaussian_pulse(193e12, 2e-15)
+    o = O.OracleFDTD(g, dt, mats, cpml_layers=4)
+    idx = g.component_indices("Ez", 15, 16, 13, 14, 12, 13)
+    o.add_source("Ez", idx, wf)
+    n = 40
+    o.run(n)
+    from prismo_gb300.pml import PMLParams
+
+    for prec in ("fp64", "fp32"):
+        eng = make_engine(g.dims, g.spacing, dt, False, precision=prec, material_arrays=mats,
+                          pml=PMLParams(thickness=4))
+        eng.add_source("Ez", eng.offsets("Ez", idx), None, wf)
+        t = np.cumsum(np.full(n, dt))
+        eng.step(n, np.array([wf(x) for x in t])[:, None])
+        out = read_fields(eng)
+        for c in COMPS:
+            tol = 1e-12 if prec == "fp64" else 1e-5
+            assert rel_l2(out[c], o.F[c]) <= tol, (prec, c, rel_l2(out[c], o.F[c]))
+        eng.close()
