@@ -221,7 +221,13 @@ def main():
     ap.add_argument("--tsteps", type=int, default=TSTEPS, help="time steps per bench step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--dims", type=int, default=None,
+                    help="cube edge for a reduced profiling case (default: the 256^3 workload)")
     args = ap.parse_args()
+    global DIMS
+    if args.dims:
+        DIMS = (args.dims,) * 3
     if args.impl == "reference":
         run_reference(args)
         return
@@ -239,7 +245,7 @@ def main():
     from prismo_gb300.workloads import boxes_3d
 
     eps = boxes_3d(DIMS, seed=0)
-    grid, eng, amps_full = make_engine(eps)
+    grid, eng, amps_full = make_engine(eps, dims=DIMS)
     tsteps = args.tsteps
     amps = amps_full[:tsteps]
     cells = float(np.prod(DIMS))
@@ -249,6 +255,7 @@ def main():
         reset(eng)
         eng.step(tsteps, amps)
 
+    tuned_chunk = None if args.no_autotune else eng.autotune(cache=False)
     for _ in range(max(args.warmup, 3)):
         one()
     eng.synchronize()
@@ -283,7 +290,7 @@ def main():
     value = cells * tsteps * args.steps * ws / (ms_total / 1e3) / 1e9
 
     # roofline of the dominant kernel (fused H+E stencil, one launch = one time step)
-    bpc = b_alg()
+    bpc = b_alg(DIMS)
     avg_launch_s = kern_ms / 1e3 / max(kern_n, 1)
     achieved = bpc * cells / avg_launch_s / 1e9  # GB/s
     peak, peak_kind = measured_peaks()
@@ -296,7 +303,7 @@ def main():
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
-        v, el = cpu_baseline_sample(nsteps=3)
+        v, el = cpu_baseline_sample(dims=DIMS, nsteps=3)
         cpu = {"value": v, "unit": "Gcell/s", "cores": 1, "kind": "port",
                "sample": f"3 time steps (of 2000) of the 256^3 CPML stepper, NumPy float64 oracle, {el:.1f} s"}
 
@@ -308,7 +315,8 @@ def main():
             "config": {"workload": "3d_fp32_cpml_256: 256^3 total cells, dx=20nm, 12-cell CPML, Courant 0.5, "
                                    "32 seeded boxes eps U[1,12.11] on 2.085, Ez dipole 193THz/10fs",
                        "time_steps_per_step": tsteps, "parallelism": "replicas" if ws > 1 else "single",
-                       "l2": "inputs larger than L2 (fields 2x403 MB)", "status": status},
+                       "l2": "inputs larger than L2 (fields 2x403 MB)", "status": status,
+                       "fused_chunk": tuned_chunk},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "bytes_per_cell_update": bpc, "kernel": "fused3 (H+E+CPML)",

@@ -129,6 +129,12 @@ int pc_status(pc_ctx* ctx, uint32_t* flags, void* stream);
 /* Number of this library's kernels launched since the context was created. */
 int64_t pc_launch_count(const pc_ctx* ctx);
 
+/* Tuning knobs (0 = automatic choice).  PC_TUNE_FUSED_CHUNK: planes along x
+ * streamed by one CTA of the fused 3D schedule. */
+#define PC_TUNE_FUSED_CHUNK 1
+int pc_set_tuning(pc_ctx* ctx, int32_t key, int64_t value);
+int64_t pc_get_tuning(const pc_ctx* ctx, int32_t key);
+
 /* Time the main stencil launch of every pc_step with a CUDA event pair on the
  * launching stream (enable != 0), and read the summed milliseconds and the
  * number of timed launches since the last read (synchronises the events). */

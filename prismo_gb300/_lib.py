@@ -31,6 +31,8 @@ PC_SCHED_AUTO = 0
 PC_SCHED_SPLIT = 1
 PC_SCHED_FUSED = 2
 
+PC_TUNE_FUSED_CHUNK = 1
+
 
 class GridDesc(C.Structure):
     _fields_ = [
@@ -72,6 +74,8 @@ SIGNATURES = {
     "pc_step": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_void_p]),
     "pc_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p]),
     "pc_launch_count": (C.c_int64, [C.c_void_p]),
+    "pc_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),
+    "pc_get_tuning": (C.c_int64, [C.c_void_p, C.c_int32]),
     "pc_profile": (C.c_int, [C.c_void_p, C.c_int32]),
     "pc_profile_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
 }

@@ -92,6 +92,7 @@ void pc_destroy(pc_ctx* c) {
     }
     cudaFree(c->d_amps);
     cudaFree(c->d_cpml_coef);
+    cudaFree(c->d_cpml_slab);
     cudaFree(c->d_status);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
     destroy_fused_state(c);
@@ -158,6 +159,7 @@ int pc_set_cpml(pc_ctx* c, int32_t t, const double* const b[3], const double* co
         c->cpml_t = 0;
         return PC_OK;
     }
+    if (t > PC_MAX_CPML) return PC_ERR_INVALID;
     if (c->g.mode == PC_MODE_LEGACY) return PC_ERR_INVALID;  // the reference has no CPML
     const pc_grid_desc& g = c->g;
     const int naxes = g.ndim;
@@ -184,10 +186,34 @@ int pc_set_cpml(pc_ctx* c, int32_t t, const double* const b[3], const double* co
             off += n[ax];
         }
     }
+    // compact copy: entries at slab index s (lower slab s < t, upper n - 2t + s)
+    std::vector<unsigned char> slab((size_t)9 * 2 * t * es, 0);
+    for (int ax = 0; ax < 3; ++ax) {
+        for (int w = 0; w < 3; ++w) {
+            for (int sidx = 0; sidx < 2 * t; ++sidx) {
+                double v = 1.0;
+                if (ax < naxes) {
+                    const int i = sidx < t ? sidx : n[ax] - 2 * t + sidx;
+                    v = w == 0 ? b[ax][i] : (w == 1 ? a[ax][i] : 1.0 / kappa[ax][i]);
+                } else if (w == 1) {
+                    v = 0.0;
+                }
+                const size_t o = ((size_t)ax * 3 + w) * 2 * t + sidx;
+                if (es == 8)
+                    ((double*)slab.data())[o] = v;
+                else
+                    ((float*)slab.data())[o] = (float)v;
+            }
+        }
+    }
     cudaFree(c->d_cpml_coef);
+    cudaFree(c->d_cpml_slab);
     c->d_cpml_coef = nullptr;
+    c->d_cpml_slab = nullptr;
     PC_CUDA_CHECK(cudaMalloc(&c->d_cpml_coef, host.size()));
     PC_CUDA_CHECK(cudaMemcpy(c->d_cpml_coef, host.data(), host.size(), cudaMemcpyHostToDevice));
+    PC_CUDA_CHECK(cudaMalloc(&c->d_cpml_slab, slab.size()));
+    PC_CUDA_CHECK(cudaMemcpy(c->d_cpml_slab, slab.data(), slab.size(), cudaMemcpyHostToDevice));
     c->cpml_t = t;
     c->psi[0] = psi0;
     c->psi[1] = psi1;
@@ -278,6 +304,24 @@ int pc_status(pc_ctx* c, uint32_t* flags, void* stream) {
 }
 
 int64_t pc_launch_count(const pc_ctx* c) { return c ? c->launches : -1; }
+
+int pc_set_tuning(pc_ctx* c, int32_t key, int64_t value) {
+    if (!c) return PC_ERR_INVALID;
+    switch (key) {
+        case PC_TUNE_FUSED_CHUNK:
+            if (value < 0 || value > c->g.nx) return PC_ERR_INVALID;
+            c->fused_cx = (int)value;
+            return PC_OK;
+        default:
+            return PC_ERR_INVALID;
+    }
+}
+
+int64_t pc_get_tuning(const pc_ctx* c, int32_t key) {
+    if (!c) return PC_ERR_INVALID;
+    if (key == PC_TUNE_FUSED_CHUNK) return c->fused_cx;
+    return PC_ERR_INVALID;
+}
 
 int pc_profile(pc_ctx* c, int32_t enable) {
     if (!c) return PC_ERR_INVALID;

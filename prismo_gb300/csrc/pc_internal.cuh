@@ -9,6 +9,7 @@
 #include "../../include/prismo_cuda.h"
 
 #define PC_MAX_SOURCES 64
+#define PC_MAX_CPML 64  // maximum CPML thickness in cells
 
 namespace pc {
 
@@ -42,10 +43,13 @@ struct CpmlArgs {
     const T* b[3];     // recursion decay, length n_axis
     const T* a[3];     // recursion gain, length n_axis
     const T* kinv[3];  // 1/kappa, length n_axis
+    const T* slabc;    // compact slab coefficients [axis][b, a, kinv][2t]
     const T* psi_in;   // read set
     T* psi_out;        // write set (== psi_in for in-place schedules)
     int64_t slot_elems[3];
     int64_t axis_base[3];
+    int64_t total;     // elements of one psi set (bounds check)
+    uint32_t* status;  // PC_STATUS_BOUNDS is set instead of an out-of-range access
 };
 
 template <typename T>
@@ -82,6 +86,7 @@ struct pc_ctx {
     int cpml_t;
     void* psi[2];
     void* d_cpml_coef;  // [3 axes][b, a, kinv][n_axis] in context precision
+    void* d_cpml_slab;  // [3 axes][b, a, kinv][2t]: the same values at slab indices only
     // sources
     std::vector<pc::SourceDesc> sources;
     double* d_amps;

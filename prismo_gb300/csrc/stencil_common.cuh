@@ -42,6 +42,10 @@ __device__ __forceinline__ T cpml3(const CpmlArgs<T>& p, int slot, const Idx3& q
     else
         po = ((int64_t)q.i * q.ny + q.j) * (2 * p.t) + s;
     po += p.axis_base[AX] + (int64_t)slot * p.slot_elems[AX];
+    if ((uint64_t)po >= (uint64_t)p.total) {  // range check: flag and skip
+        atomicOr(p.status, PC_STATUS_BOUNDS);
+        return d;
+    }
     const T psi = p.b[AX][idx] * p.psi_in[po] + p.a[AX][idx] * d;
     p.psi_out[po] = psi;
     return d * p.kinv[AX][idx] + psi;
@@ -59,6 +63,10 @@ __device__ __forceinline__ T cpml2(const CpmlArgs<T>& p, int slot, const Idx2& q
     else
         po = (int64_t)q.i * (2 * p.t) + s;
     po += p.axis_base[AX] + (int64_t)slot * p.slot_elems[AX];
+    if ((uint64_t)po >= (uint64_t)p.total) {  // range check: flag and skip
+        atomicOr(p.status, PC_STATUS_BOUNDS);
+        return d;
+    }
     const T psi = p.b[AX][idx] * p.psi_in[po] + p.a[AX][idx] * d;
     p.psi_out[po] = psi;
     return d * p.kinv[AX][idx] + psi;
@@ -114,6 +122,9 @@ static CpmlArgs<T> make_cpml_args(pc_ctx* c, int in_set, int out_set) {
         p.slot_elems[ax] = L.slot_elems[ax];
         p.axis_base[ax] = L.axis_base[ax];
     }
+    p.total = L.total;
+    p.status = c->d_status;
+    p.slabc = static_cast<const T*>(c->d_cpml_slab);
     p.psi_in = static_cast<const T*>(c->psi[in_set] ? c->psi[in_set] : c->psi[0]);
     p.psi_out = static_cast<T*>(c->psi[out_set] ? c->psi[out_set] : c->psi[0]);
     return p;

@@ -15,6 +15,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <cmath>
 
 #include "pc_internal.cuh"
 #include "stencil_common.cuh"
@@ -25,83 +26,96 @@ namespace pc {
 struct FusedMaps {
     CUtensorMap e[3];
     CUtensorMap h[3];
-    CUtensorMap cb[3];
 };
 
 namespace {
 
 constexpr uint32_t kWaitLimit = 1u << 22;
 
+// Tile geometry: a CTA updates a TY x TZ tile of (j, k) for every plane of its
+// x-chunk.  Eight consumer warps own the tile (lane = k, RPT rows per thread);
+// a ninth helper warp issues the TMA loads and computes the 2*TZ+... halo H
+// points (row j0+TY and column k0+TZ) that the E update needs.
 template <typename T, int TY, int TZ>
 struct FusedGeom {
     static constexpr int EW = TZ + 8;  // E box: k in [k0-4, k0+TZ+4)
     static constexpr int EH = TY + 2;  //        j in [j0-1, j0+TY+1)
     static constexpr int HW = TZ + 4;  // H box: k in [k0, k0+TZ+4)
     static constexpr int HH = TY + 1;  //        j in [j0, j0+TY+1)
-    static constexpr int CW = TZ;      // Cb box: the tile
-    static constexpr int CH = TY;
+    static constexpr int NW = TZ + 1;  // H^{n+1/2} smem row stride
     static constexpr int align128(int b) { return (b + 127) / 128 * 128; }
     static constexpr int E_BOX = align128(EW * EH * (int)sizeof(T));
     static constexpr int H_BOX = align128(HW * HH * (int)sizeof(T));
-    static constexpr int C_BOX = align128(CW * CH * (int)sizeof(T));
-    static constexpr int STAGE = 3 * (E_BOX + H_BOX + C_BOX);
-    static constexpr uint32_t TX_BYTES = 3u * (EW * EH + HW * HH + CW * CH) * sizeof(T);
-    static constexpr int HN_PLANE = 3 * HH * HW;  // elements of one H^{n+1/2} plane (3 comps)
+    static constexpr int STAGE = 3 * (E_BOX + H_BOX);
+    static constexpr uint32_t TX_BYTES = 3u * (EW * EH + HW * HH) * sizeof(T);
+    static constexpr int HN_PLANE = 3 * HH * NW;  // elements of one H^{n+1/2} plane (3 comps)
+    static constexpr int NHALO = (TZ + 1) + TY;   // halo H points per plane
 };
 
 template <typename T, int TY, int TZ, int S>
 constexpr int fused_smem_bytes() {
     using G = FusedGeom<T, TY, TZ>;
-    return 128 + S * G::STAGE + 2 * G::HN_PLANE * (int)sizeof(T);
+    return 256 + S * G::STAGE + 3 * G::HN_PLANE * (int)sizeof(T);
 }
 
-template <typename T, int AX>
-__device__ __forceinline__ T cpml3w(const CpmlArgs<T>& p, int slot, const Idx3& q, T d, bool write) {
-    const int idx = AX == 0 ? q.i : (AX == 1 ? q.j : q.k);
-    const int n = AX == 0 ? q.nx : (AX == 1 ? q.ny : q.nz);
-    const int s = slab_of(idx, n, p.t);
-    if (s < 0) return d;
-    int64_t po;
-    if (AX == 0)
-        po = ((int64_t)s * q.ny + q.j) * q.pitch + q.k;
-    else if (AX == 1)
-        po = ((int64_t)q.i * (2 * p.t) + s) * q.pitch + q.k;
-    else
-        po = ((int64_t)q.i * q.ny + q.j) * (2 * p.t) + s;
-    po += p.axis_base[AX] + (int64_t)slot * p.slot_elems[AX];
-    const T psi = p.b[AX][idx] * p.psi_in[po] + p.a[AX][idx] * d;
-    if (write) p.psi_out[po] = psi;
-    return d * p.kinv[AX][idx] + psi;
+// One CPML recursion step: psi' = b psi + a d; returns kinv d + psi'.
+template <typename T>
+__device__ __forceinline__ T pstep(T b, T a, T kinv, T d, T& psi) {
+    psi = b * psi + a * d;
+    return d * kinv + psi;
 }
 
-template <typename T, int TY, int TZ, int S, bool CPML>
-__global__ void __launch_bounds__(TY* TZ, 2)
-    fused3(FieldArgs<T> a, CpmlArgs<T> pm, int cx, const __grid_constant__ FusedMaps maps) {
+// CPML state of one point: slab indices, the six psi values (slot order xA, xB,
+// yA, yB, zA, zB) and the 32-bit offsets of its x, y, z psi entries (slot 0).
+template <typename T>
+struct PsiPoint {
+    int sx, sy, sz;
+    int ox, oy, oz;
+};
+
+// RPT = 2 rows per consumer thread: rows warp and warp + TY/2 of the tile.
+template <typename T, int TY, int TZ, int S, bool CPML, bool HCOEF, bool CA>
+__global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
+    fused3(FieldArgs<T> a, CpmlArgs<T> pm, const int4* __restrict__ items, const __grid_constant__ FusedMaps maps) {
     using G = FusedGeom<T, TY, TZ>;
-    constexpr int EW = G::EW, HW = G::HW, CW = G::CW;
-    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr int EW = G::EW, HW = G::HW, NW = G::NW;
+    constexpr int NWC = TY / 2;  // consumer warps
+    static_assert(TZ == 32, "one warp spans the tile in k");
+    static_assert(S >= 3, "stage n-2 is recycled while stages n-1 and n are in use");
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    // explicit 128-byte alignment of every TMA destination
+    unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem);
     unsigned char* stages = smem + 128;
     T* sHn = reinterpret_cast<T*>(stages + S * G::STAGE);
+    T* sC = sHn + 3 * G::HN_PLANE;  // CPML slab coefficients [axis][b, a, kinv][2t]
 
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = ty * TZ + tx;
-    const int k0 = blockIdx.x * TZ, j0 = blockIdx.y * TY;
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const int tid = warp * 32 + lane;
+    const bool helper = warp == NWC;
+    // work item: (k0, j0, first plane, one past the last plane), longest first
+    const int4 item = items[blockIdx.x];
+    const int k0 = item.x, j0 = item.y;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
-    const int ib = blockIdx.z * cx;
-    const int ie = min(nx, ib + cx);
+    const int ib = item.z;
+    const int ie = item.w;
     const int L = ie - ib + 2;  // planes ib-1 .. ie
     const int64_t P = a.pitch;
+    const int64_t PR = (int64_t)ny * P;  // plane stride
+    const int t = CPML ? pm.t : 0;
+    const int t2 = 2 * t;
+    const T idx_ = a.inv_dx, idy = a.inv_dy, idz = a.inv_dz;
 
-    if (tid == 0) {
+    if (helper && lane == 0) {
         for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
         fence_mbar_init();
         for (int c = 0; c < 3; ++c) {
             prefetch_tmap(&maps.e[c]);
             prefetch_tmap(&maps.h[c]);
-            prefetch_tmap(&maps.cb[c]);
         }
     }
+    if (CPML)
+        for (int i = tid; i < 9 * t2; i += blockDim.x * blockDim.y) sC[i] = pm.slabc[i];
     __syncthreads();
 
     auto issue = [&](int n) {
@@ -114,151 +128,324 @@ __global__ void __launch_bounds__(TY* TZ, 2)
 #pragma unroll
         for (int c = 0; c < 3; ++c)
             tma_load_3d(st + 3 * G::E_BOX + c * G::H_BOX, &maps.h[c], k0, j0, pl, &bars[s]);
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-            tma_load_3d(st + 3 * (G::E_BOX + G::H_BOX) + c * G::C_BOX, &maps.cb[c], k0, j0, pl, &bars[s]);
     };
     int issued = L < S ? L : S;
-    if (tid == 0)
+    if (helper && lane == 0)
         for (int n = 0; n < issued; ++n) issue(n);
 
-    auto Ebox = [&](int n, int c) {
-        return reinterpret_cast<const T*>(stages + (n % S) * G::STAGE + c * G::E_BOX);
+    // ---- CPML bookkeeping (32-bit offsets: the host guarantees psi < 2^31 elements) ----
+    const int P32 = (int)P;
+    const int se0 = (int)pm.slot_elems[0], se1 = (int)pm.slot_elems[1], se2 = (int)pm.slot_elems[2];
+    const int tot = (int)pm.total;
+    auto sl_of = [&](int i, int nn) { return (CPML && i >= 0 && i < nn) ? slab_of(i, nn, t) : -1; };
+    // coefficient triplet (b, a, kinv) of slab index sl on axis ax (1, 0, 1 outside)
+    auto coef3 = [&](int ax, int sl, T& b, T& aa, T& kk) {
+        if (sl >= 0) {
+            b = sC[(ax * 3 + 0) * t2 + sl];
+            aa = sC[(ax * 3 + 1) * t2 + sl];
+            kk = sC[(ax * 3 + 2) * t2 + sl];
+        } else {
+            b = T(1), aa = T(0), kk = T(1);
+        }
     };
-    auto Hbox = [&](int n, int c) {
-        return reinterpret_cast<const T*>(stages + (n % S) * G::STAGE + 3 * G::E_BOX + c * G::H_BOX);
+    auto ld = [&](int o) -> T {
+        if ((unsigned)o >= (unsigned)tot) {  // range check: flag and skip
+            atomicOr(pm.status, PC_STATUS_BOUNDS);
+            return T(0);
+        }
+        return __ldg(pm.psi_in + o);
     };
-    auto Cbox = [&](int n, int c) {
-        return reinterpret_cast<const T*>(stages + (n % S) * G::STAGE + 3 * (G::E_BOX + G::H_BOX) + c * G::C_BOX);
+    auto st = [&](int o, T v) {
+        if ((unsigned)o >= (unsigned)tot) {
+            atomicOr(pm.status, PC_STATUS_BOUNDS);
+            return;
+        }
+        pm.psi_out[o] = v;
     };
-    auto Hn = [&](int plane, int c) { return sHn + (plane & 1) * G::HN_PLANE + c * (G::HH * HW); };
+    // point state for plane pl of a point (j, k) with per-point constants
+    // (syc, szc: slab indices; oyc/ozc: plane-independent parts of the offsets)
+    auto make_pt = [&](int pl, int sxp, int syc, int szc, int oxc, int oyc, int ozc) {
+        PsiPoint<T> q;
+        const bool pv = pl >= 0 && pl < nx;
+        q.sx = pv ? sxp : -1;
+        q.sy = pv ? syc : -1;
+        q.sz = pv ? szc : -1;
+        q.ox = oxc + (q.sx >= 0 ? q.sx : 0) * (ny * P32);
+        q.oy = oyc + pl * (t2 * P32);
+        q.oz = ozc + pl * (ny * t2);
+        return q;
+    };
+    // slot offsets of H and E psi entries inside an axis block
+    const int xA_H = SX_HY * se0, xB_H = SX_HZ * se0, yA_H = SY_HX * se1, yB_H = SY_HZ * se1;
+    const int zA_H = SZ_HX * se2, zB_H = SZ_HY * se2;
+    const int xA_E = SX_EY * se0, xB_E = SX_EZ * se0, yA_E = SY_EX * se1, yB_E = SY_EZ * se1;
+    const int zA_E = SZ_EX * se2, zB_E = SZ_EY * se2;
+    auto fetch = [&](const PsiPoint<T>& q, bool isH, T* v) {
+#pragma unroll
+        for (int w = 0; w < 6; ++w) v[w] = T(0);
+        if (q.sx >= 0) {
+            v[0] = ld(q.ox + (isH ? xA_H : xA_E));
+            v[1] = ld(q.ox + (isH ? xB_H : xB_E));
+        }
+        if (q.sy >= 0) {
+            v[2] = ld(q.oy + (isH ? yA_H : yA_E));
+            v[3] = ld(q.oy + (isH ? yB_H : yB_E));
+        }
+        if (q.sz >= 0) {
+            v[4] = ld(q.oz + (isH ? zA_H : zA_E));
+            v[5] = ld(q.oz + (isH ? zB_H : zB_E));
+        }
+    };
 
-    // H^{n+1/2} at (p, j0+jj, k0+kk) into shared memory; psi written only when own.
-    auto h_point = [&](int n, int p, int jj, int kk, bool own) {
-        const int j = j0 + jj, k = k0 + kk;
-        const int ho = jj * HW + kk;
-        const int ei = (jj + 1) * EW + (kk + 4);
-        const T* Exc = Ebox(n, 0);
-        const T* Eyc = Ebox(n, 1);
-        const T* Ezc = Ebox(n, 2);
-        const T* Eyp = Ebox(n - 1, 1);
-        const T* Ezp = Ebox(n - 1, 2);
-        T hx = Hbox(n, 0)[ho], hy = Hbox(n, 1)[ho], hz = Hbox(n, 2)[ho];
-        const Idx3 q{p, j, k, nx, ny, nz, a.pitch};
-        const int64_t o = ((int64_t)p * ny + j) * P + k;
-        if (p < nx - 1 && j >= 1 && j <= ny - 2 && k >= 1 && k <= nz - 2) {
-            T cy = (Ezc[ei] - Ezc[ei - EW]) * a.inv_dy;
-            T cz = (Eyc[ei] - Eyc[ei - 1]) * a.inv_dz;
-            if (CPML) {
-                cy = cpml3w<T, 1>(pm, SY_HX, q, cy, own);
-                cz = cpml3w<T, 2>(pm, SZ_HX, q, cz, own);
-            }
-            hx = hcoef(a.da[0], o, a.da_s) * hx - hcoef(a.db[0], o, a.db_s) * (cy - cz);
+    // ---- per-thread points -------------------------------------------------
+    // Consumers own rows (warp, warp + TY/2) at lane k; the helper owns the two halo
+    // points h = lane, lane + 32 (row j0+TY, then column k0+TZ).  Same registers.
+    int pj[2], pk[2], pei[2], pho[2], pno[2], psy[2], psz[2], poxc[2], poyc[2], pozc[2];
+    bool pin[2];  // point exists and lies inside the domain
+    T pyb[2], pya[2], pyk[2], pzb[2], pza[2], pzk[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        int jj, kk;
+        bool exists = true;
+        if (!helper) {
+            jj = warp + NWC * r;
+            kk = lane;
+        } else {
+            const int h = lane + 32 * r;
+            exists = h < G::NHALO;
+            jj = h <= TZ ? TY : h - (TZ + 1);
+            kk = h <= TZ ? h : TZ;
         }
-        if (p >= 1 && p <= nx - 2 && j <= ny - 2 && k >= 1 && k <= nz - 2) {
-            T cz = (Exc[ei] - Exc[ei - 1]) * a.inv_dz;
-            T cx_ = (Ezc[ei] - Ezp[ei]) * a.inv_dx;
-            if (CPML) {
-                cz = cpml3w<T, 2>(pm, SZ_HY, q, cz, own);
-                cx_ = cpml3w<T, 0>(pm, SX_HY, q, cx_, own);
+        pj[r] = j0 + jj;
+        pk[r] = k0 + kk;
+        pei[r] = (jj + 1) * EW + (kk + 4);
+        pho[r] = jj * HW + kk;
+        pno[r] = jj * NW + kk;
+        pin[r] = exists && pj[r] < ny && pk[r] < nz;
+        psy[r] = pin[r] ? sl_of(pj[r], ny) : -1;
+        psz[r] = pin[r] ? sl_of(pk[r], nz) : -1;
+        coef3(1, psy[r], pyb[r], pya[r], pyk[r]);
+        coef3(2, psz[r], pzb[r], pza[r], pzk[r]);
+        poxc[r] = (int)pm.axis_base[0] + pj[r] * P32 + pk[r];
+        poyc[r] = (int)pm.axis_base[1] + (psy[r] >= 0 ? psy[r] : 0) * P32 + pk[r];
+        pozc[r] = (int)pm.axis_base[2] + pj[r] * t2 + (psz[r] >= 0 ? psz[r] : 0);
+    }
+    const int k = k0 + lane;  // consumers' own k
+    auto pt_at = [&](int pl, int r) {
+        return make_pt(pl, pin[r] ? sl_of(pl, nx) : -1, psy[r], psz[r], poxc[r], poyc[r], pozc[r]);
+    };
+    auto og = [&](int pl, int r) { return (int64_t)pl * PR + (int64_t)pj[r] * P + pk[r]; };
+    // CTA-uniform: does the tile touch a y or z slab (then every plane needs CPML)?
+    const bool yz_slab = CPML && (j0 < t || j0 + TY > ny - t || k0 < t || k0 + TZ > nz - t);
+    auto x_slab = [&](int pl) { return CPML && pl >= 0 && pl < nx && (pl < t || pl >= nx - t); };
+
+    // ---- H^{n+1/2} at one point --------------------------------------------
+    auto h_compute = [&](const T* E0, const T* E1, const T* E2, const T* Ep1, const T* Ep2, const T* H0,
+                         const T* H1, const T* H2, int ei, int ho, int p, int j, int kk, bool own, bool slab,
+                         const PsiPoint<T>& q, T xb, T xa, T xk, T b1, T a1, T k1, T b2, T a2, T k2, T* v,
+                         int64_t og, T& hx, T& hy, T& hz) {
+        const bool pin = p >= 1 && p <= nx - 2;
+        const bool jin = j >= 1 && j <= ny - 2;
+        const bool kin = kk >= 1 && kk <= nz - 2;
+        const bool ux = p >= 0 && p <= nx - 2 && jin && kin;
+        const bool uy = pin && j <= ny - 2 && kin;
+        const bool uz = pin && jin && kk <= nz - 2;
+        const T ez = E2[ei], ey = E1[ei], ex = E0[ei];
+        // derivatives in psi slot order: (dEz/dx Hy, dEy/dx Hz, dEz/dy Hx, dEx/dy Hz, dEy/dz Hx, dEx/dz Hy)
+        T d0 = (ez - Ep2[ei]) * idx_;
+        T d1 = (ey - Ep1[ei]) * idx_;
+        T d2 = (ez - E2[ei - EW]) * idy;
+        T d3 = (ex - E0[ei - EW]) * idy;
+        T d4 = (ey - E1[ei - 1]) * idz;
+        T d5 = (ex - E0[ei - 1]) * idz;
+        if (CPML && slab) {
+            if (q.sx >= 0) {
+                d0 = pstep(xb, xa, xk, d0, v[0]);
+                d1 = pstep(xb, xa, xk, d1, v[1]);
+                if (own && uy) st(q.ox + xA_H, v[0]);
+                if (own && uz) st(q.ox + xB_H, v[1]);
             }
-            hy = hcoef(a.da[1], o, a.da_s) * hy - hcoef(a.db[1], o, a.db_s) * (cz - cx_);
-        }
-        if (p >= 1 && p <= nx - 2 && j >= 1 && j <= ny - 2 && k <= nz - 2) {
-            T cx_ = (Eyc[ei] - Eyp[ei]) * a.inv_dx;
-            T cy = (Exc[ei] - Exc[ei - EW]) * a.inv_dy;
-            if (CPML) {
-                cx_ = cpml3w<T, 0>(pm, SX_HZ, q, cx_, own);
-                cy = cpml3w<T, 1>(pm, SY_HZ, q, cy, own);
+            if (q.sy >= 0) {
+                d2 = pstep(b1, a1, k1, d2, v[2]);
+                d3 = pstep(b1, a1, k1, d3, v[3]);
+                if (own && ux) st(q.oy + yA_H, v[2]);
+                if (own && uz) st(q.oy + yB_H, v[3]);
             }
-            hz = hcoef(a.da[2], o, a.da_s) * hz - hcoef(a.db[2], o, a.db_s) * (cx_ - cy);
+            if (q.sz >= 0) {
+                d4 = pstep(b2, a2, k2, d4, v[4]);
+                d5 = pstep(b2, a2, k2, d5, v[5]);
+                if (own && ux) st(q.oz + zA_H, v[4]);
+                if (own && uy) st(q.oz + zB_H, v[5]);
+            }
         }
-        Hn(p, 0)[ho] = hx;
-        Hn(p, 1)[ho] = hy;
-        Hn(p, 2)[ho] = hz;
+        hx = H0[ho];
+        hy = H1[ho];
+        hz = H2[ho];
+        T da0 = a.da_s, da1 = a.da_s, da2 = a.da_s, db0 = a.db_s, db1 = a.db_s, db2 = a.db_s;
+        if (HCOEF) {
+            if (ux) da0 = a.da[0][og], db0 = a.db[0][og];
+            if (uy) da1 = a.da[1][og], db1 = a.db[1][og];
+            if (uz) da2 = a.da[2][og], db2 = a.db[2][og];
+        }
+        if (ux) hx = da0 * hx - db0 * (d2 - d4);
+        if (uy) hy = da1 * hy - db1 * (d5 - d0);
+        if (uz) hz = da2 * hz - db2 * (d1 - d3);
     };
 
     bool timed_out = false;
     int n = 0;
+    int sn = 0, sp = S - 1;  // stage of plane n and n-1
+    int hc = 0, hp = 2;      // H^{n+1/2} smem buffer of plane n and n-1
+    T pfH[2][6], pfE[2][6];  // psi prefetched one plane ahead (slab planes only)
+    if (CPML && (yz_slab || x_slab(ib))) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) fetch(pt_at(ib, r), true, pfH[r]);
+    }
+    T chk = T(0);  // running sum of E^{n+1}: non-finite iff some value was
     for (; n < L; ++n) {
-        const bool ok = mbar_wait_bounded(&bars[n % S], (uint32_t)((n / S) & 1), kWaitLimit);
-        const int pc_ = ib - 1 + n;  // plane whose H^{n+1/2} is computed now
+        const int p = ib - 1 + n;  // plane whose H^{n+1/2} is computed now
+        const int q = p - 1;       // plane whose E^{n+1} is computed now
+        const bool slabH = yz_slab || x_slab(p);
+        const bool slabE = yz_slab || x_slab(q);
+        const unsigned char* stc = stages + sn * G::STAGE;
+        const unsigned char* stp = stages + sp * G::STAGE;
+        const T* Ec0 = reinterpret_cast<const T*>(stc);
+        const T* Ec1 = reinterpret_cast<const T*>(stc + G::E_BOX);
+        const T* Ec2 = reinterpret_cast<const T*>(stc + 2 * G::E_BOX);
+        const T* Hc0 = reinterpret_cast<const T*>(stc + 3 * G::E_BOX);
+        const T* Hc1 = reinterpret_cast<const T*>(stc + 3 * G::E_BOX + G::H_BOX);
+        const T* Hc2 = reinterpret_cast<const T*>(stc + 3 * G::E_BOX + 2 * G::H_BOX);
+        const T* Ep0 = reinterpret_cast<const T*>(stp);
+        const T* Ep1 = reinterpret_cast<const T*>(stp + G::E_BOX);
+        const T* Ep2 = reinterpret_cast<const T*>(stp + 2 * G::E_BOX);
+        T* Nc0 = sHn + hc * G::HN_PLANE;
+        T* Nc1 = Nc0 + G::HH * NW;
+        T* Nc2 = Nc1 + G::HH * NW;
+        const T* Np0 = sHn + hp * G::HN_PLANE;
+        const T* Np1 = Np0 + G::HH * NW;
+        const T* Np2 = Np1 + G::HH * NW;
+        // prefetch Cb(q) for the E update while the H phase runs
+        T cb[2][3];
+        if (!helper && n >= 2) {
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const int64_t o = og(q, r);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) cb[r][c] = pin[r] ? __ldg(a.cb[c] + o) : T(0);
+            }
+        }
+        // x-slab coefficients of planes p and q (uniform)
+        T xbH = T(1), xaH = T(0), xkH = T(1), xbE = T(1), xaE = T(0), xkE = T(1);
+        if (CPML) {
+            coef3(0, sl_of(p, nx), xbH, xaH, xkH);
+            coef3(0, sl_of(q, nx), xbE, xaE, xkE);
+        }
+        const bool ok = mbar_wait_bounded(&bars[sn], (uint32_t)((n / S) & 1), kWaitLimit);
+        T hv[2][3];
         if (n >= 1 && ok) {
-            h_point(n, pc_, ty, tx, pc_ < ie);
-            if (tid < TZ + 1)
-                h_point(n, pc_, TY, tid, false);
-            else if (tid < TZ + 1 + TY)
-                h_point(n, pc_, tid - (TZ + 1), TZ, false);
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                if (helper && lane + 32 * r >= G::NHALO) continue;
+                const PsiPoint<T> pt = pt_at(p, r);
+                h_compute(Ec0, Ec1, Ec2, Ep1, Ep2, Hc0, Hc1, Hc2, pei[r], pho[r], p, pj[r], pk[r],
+                          !helper && p < ie, slabH, pt, xbH, xaH, xkH, pyb[r], pya[r], pyk[r], pzb[r], pza[r],
+                          pzk[r], pfH[r], og(p, r), hv[r][0], hv[r][1], hv[r][2]);
+                Nc0[pno[r]] = hv[r][0];
+                Nc1[pno[r]] = hv[r][1];
+                Nc2[pno[r]] = hv[r][2];
+            }
         }
         if (__syncthreads_or(!ok)) {
             timed_out = true;
             break;
         }
-        const int j = j0 + ty, k = k0 + tx;
-        const bool inside = j < ny && k < nz;
-        if (n >= 2) {
-            // E^{n+1} at plane q = pc_ - 1, own point
-            const int q = pc_ - 1;
-            const int ei = (ty + 1) * EW + (tx + 4);
-            const int hi = ty * HW + tx;
-            const int ci = ty * CW + tx;
-            const T* Hxq = Hn(q, 0);
-            const T* Hyq = Hn(q, 1);
-            const T* Hzq = Hn(q, 2);
-            const T* Hyp = Hn(pc_, 1);
-            const T* Hzp = Hn(pc_, 2);
-            T ex = Ebox(n - 1, 0)[ei], ey = Ebox(n - 1, 1)[ei], ez = Ebox(n - 1, 2)[ei];
-            const Idx3 qq{q, j, k, nx, ny, nz, a.pitch};
-            const int64_t o = ((int64_t)q * ny + j) * P + k;
-            if (j <= ny - 2 && k <= nz - 2) {
-                T c1 = (Hzq[hi + HW] - Hzq[hi]) * a.inv_dy;
-                T c2 = (Hyq[hi + 1] - Hyq[hi]) * a.inv_dz;
-                if (CPML) {
-                    c1 = cpml3w<T, 1>(pm, SY_EX, qq, c1, true);
-                    c2 = cpml3w<T, 2>(pm, SZ_EX, qq, c2, true);
-                }
-                ex = ecoef(a.ca[0], o) * ex + Cbox(n - 1, 0)[ci] * (c1 - c2);
-            }
-            if (q <= nx - 2 && k <= nz - 2) {
-                T c1 = (Hxq[hi + 1] - Hxq[hi]) * a.inv_dz;
-                T c2 = (Hzp[hi] - Hzq[hi]) * a.inv_dx;
-                if (CPML) {
-                    c1 = cpml3w<T, 2>(pm, SZ_EY, qq, c1, true);
-                    c2 = cpml3w<T, 0>(pm, SX_EY, qq, c2, true);
-                }
-                ey = ecoef(a.ca[1], o) * ey + Cbox(n - 1, 1)[ci] * (c1 - c2);
-            }
-            if (q <= nx - 2 && j <= ny - 2) {
-                T c1 = (Hyp[hi] - Hyq[hi]) * a.inv_dx;
-                T c2 = (Hxq[hi + HW] - Hxq[hi]) * a.inv_dy;
-                if (CPML) {
-                    c1 = cpml3w<T, 0>(pm, SX_EZ, qq, c1, true);
-                    c2 = cpml3w<T, 1>(pm, SY_EZ, qq, c2, true);
-                }
-                ez = ecoef(a.ca[2], o) * ez + Cbox(n - 1, 2)[ci] * (c1 - c2);
-            }
-            if (inside) {
-                a.Eout[0][o] = ex;
-                a.Eout[1][o] = ey;
-                a.Eout[2][o] = ez;
-                if (!(isfinite(ex) && isfinite(ey) && isfinite(ez))) atomicOr(a.status, PC_STATUS_NONFINITE);
-            }
-        }
-        if (n >= 1 && pc_ < ie && inside) {
-            const int64_t o = ((int64_t)pc_ * ny + j) * P + k;
-            const int hi = ty * HW + tx;
-            a.Hout[0][o] = Hn(pc_, 0)[hi];
-            a.Hout[1][o] = Hn(pc_, 1)[hi];
-            a.Hout[2][o] = Hn(pc_, 2)[hi];
-        }
-        __syncthreads();
-        if (n >= 1 && n - 1 + S < L) {
-            if (tid == 0) issue(n - 1 + S);
+        if (n >= 2 && n - 2 + S < L) {
+            if (helper && lane == 0) issue(n - 2 + S);
             ++issued;
         }
+        // H-phase psi of the next plane: issued now so the loads overlap the E phase
+        if (CPML && (yz_slab || x_slab(p + 1))) {
+#pragma unroll
+            for (int r = 0; r < 2; ++r) fetch(pt_at(p + 1, r), true, pfH[r]);
+        }
+        if (!helper) {
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const int j = pj[r];
+                if (!pin[r]) continue;
+                if (n >= 2) {
+                    const int no = pno[r];
+                    const bool ux = j <= ny - 2 && k <= nz - 2;
+                    const bool uy = q <= nx - 2 && k <= nz - 2;
+                    const bool uz = q <= nx - 2 && j <= ny - 2;
+                    const T hxq = Np0[no], hyq = Np1[no], hzq = Np2[no];
+                    // derivatives in psi slot order:
+                    // (dHz/dx Ey, dHy/dx Ez, dHz/dy Ex, dHx/dy Ez, dHy/dz Ex, dHx/dz Ey)
+                    T d0 = (Nc2[no] - hzq) * idx_;
+                    T d1 = (Nc1[no] - hyq) * idx_;
+                    T d2 = (Np2[no + NW] - hzq) * idy;
+                    T d3 = (Np0[no + NW] - hxq) * idy;
+                    T d4 = (Np1[no + 1] - hyq) * idz;
+                    T d5 = (Np0[no + 1] - hxq) * idz;
+                    if (CPML && slabE) {
+                        const PsiPoint<T> pt = pt_at(q, r);
+                        T* v = pfE[r];
+                        if (pt.sx >= 0) {
+                            d0 = pstep(xbE, xaE, xkE, d0, v[0]);
+                            d1 = pstep(xbE, xaE, xkE, d1, v[1]);
+                            if (uy) st(pt.ox + xA_E, v[0]);
+                            if (uz) st(pt.ox + xB_E, v[1]);
+                        }
+                        if (pt.sy >= 0) {
+                            d2 = pstep(pyb[r], pya[r], pyk[r], d2, v[2]);
+                            d3 = pstep(pyb[r], pya[r], pyk[r], d3, v[3]);
+                            if (ux) st(pt.oy + yA_E, v[2]);
+                            if (uz) st(pt.oy + yB_E, v[3]);
+                        }
+                        if (pt.sz >= 0) {
+                            d4 = pstep(pzb[r], pza[r], pzk[r], d4, v[4]);
+                            d5 = pstep(pzb[r], pza[r], pzk[r], d5, v[5]);
+                            if (ux) st(pt.oz + zA_E, v[4]);
+                            if (uy) st(pt.oz + zB_E, v[5]);
+                        }
+                    }
+                    const int ei = pei[r];
+                    T ex = Ep0[ei], ey = Ep1[ei], ez = Ep2[ei];
+                    const int64_t o = og(q, r);
+                    T ca0 = T(1), ca1 = T(1), ca2 = T(1);
+                    if (CA) {
+                        ca0 = a.ca[0][o];
+                        ca1 = a.ca[1][o];
+                        ca2 = a.ca[2][o];
+                    }
+                    if (ux) ex = ca0 * ex + cb[r][0] * (d2 - d4);
+                    if (uy) ey = ca1 * ey + cb[r][1] * (d5 - d0);
+                    if (uz) ez = ca2 * ez + cb[r][2] * (d1 - d3);
+                    a.Eout[0][o] = ex;
+                    a.Eout[1][o] = ey;
+                    a.Eout[2][o] = ez;
+                    chk += (ex + ey) + ez;
+                }
+                if (n >= 1 && p < ie) {
+                    const int64_t o = og(p, r);
+                    a.Hout[0][o] = hv[r][0];
+                    a.Hout[1][o] = hv[r][1];
+                    a.Hout[2][o] = hv[r][2];
+                }
+            }
+            if (CPML && n >= 1 && (yz_slab || x_slab(p))) {  // E-phase psi of the next iteration
+#pragma unroll
+                for (int r = 0; r < 2; ++r) fetch(pt_at(p, r), false, pfE[r]);
+            }
+        }
+        sp = sn;
+        sn = (sn + 1 == S) ? 0 : sn + 1;
+        hp = hc;
+        hc = (hc + 1 == 3) ? 0 : hc + 1;
     }
+    if (!helper && !isfinite(chk)) atomicOr(a.status, PC_STATUS_NONFINITE);
     if (timed_out) {
-        if (tid == 0) atomicOr(a.status, PC_STATUS_TIMEOUT);
+        if (helper && lane == 0) atomicOr(a.status, PC_STATUS_TIMEOUT);
         // let every copy already in flight land before the CTA retires
         for (int m = n; m < issued; ++m) mbar_wait_bounded(&bars[m % S], (uint32_t)((m / S) & 1), kWaitLimit);
     }
@@ -291,22 +478,100 @@ int make_map(CUtensorMap* m, const void* base, const pc_grid_desc& g, int bw, in
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = enc(m, es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
                      const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? PC_OK : PC_ERR_CUDA;
 }
 
 struct FusedState {
     const void* key_f[2][6];
-    const void* key_cb[3];
     FusedMaps maps[2];  // per input set
     bool ready = false;
+    int4* d_items = nullptr;  // work items of the current chunking
+    int n_items = 0, items_cx = -1, items_t = -1;
 };
 
 // One cached set of maps per context (keyed by the buffer pointers).
 FusedState* state_of(pc_ctx* c) {
     if (!c->fused_state) c->fused_state = new FusedState();
     return static_cast<FusedState*>(c->fused_state);
+}
+
+// Work items (k0, j0, ib, ie) for a chunk length cx, most expensive first: tiles
+// that touch a y/z CPML slab run the psi path on every plane, the others only on
+// x-slab planes (longest-processing-time-first ordering against the tail).
+static std::vector<int4> fused_items(const pc_grid_desc& g, int TY, int TZ, int cx, int t) {
+    std::vector<std::pair<double, int4>> v;
+    for (int ib = 0; ib < g.nx; ib += cx) {
+        const int ie = std::min(g.nx, ib + cx);
+        int xs = 0;
+        for (int p = ib; p < ie; ++p) xs += (t > 0 && (p < t || p >= g.nx - t)) ? 1 : 0;
+        for (int j0 = 0; j0 < g.ny; j0 += TY)
+            for (int k0 = 0; k0 < g.nz; k0 += TZ) {
+                const bool yz = t > 0 && (j0 < t || j0 + TY > g.ny - t || k0 < t || k0 + TZ > g.nz - t);
+                const int planes = ie - ib + 2;
+                const double cost = yz ? 3.0 * planes : (planes + 2.0 * xs);
+                v.push_back({cost, make_int4(k0, j0, ib, ie)});
+            }
+    }
+    std::stable_sort(v.begin(), v.end(), [](const std::pair<double, int4>& x, const std::pair<double, int4>& y) {
+        return x.first > y.first;
+    });
+    std::vector<int4> out;
+    out.reserve(v.size());
+    for (auto& e : v) out.push_back(e.second);
+    return out;
+}
+
+template <typename T, int TY, int TZ, int S, bool CPML, bool HCOEF, bool CA>
+int launch_variant(pc_ctx* c, cudaStream_t s, const FieldArgs<T>& a, const CpmlArgs<T>& p, const FusedMaps& maps,
+                   int smem, FusedState* st) {
+    const pc_grid_desc& g = c->g;
+    auto kern = fused3<T, TY, TZ, S, CPML, HCOEF, CA>;
+    static bool attr = false;
+    if (!attr) {
+        PC_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr = true;
+    }
+    constexpr int threads = TZ * (TY / 2 + 1);
+    int cx = c->fused_cx;
+    if (cx <= 0) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+        if (sms <= 0) sms = 152;
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+        if (per_sm <= 0) per_sm = 1;
+        const int resident = sms * per_sm;
+        const int tiles = ((g.nz + TZ - 1) / TZ) * ((g.ny + TY - 1) / TY);
+        // enough items for ~8 per resident slot, with at most ~12% pipeline overhead
+        cx = g.nx;
+        const int cands[] = {16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512};
+        for (int cand : cands) {
+            if (cand >= g.nx) break;
+            const double items = (double)tiles * ((g.nx + cand - 1) / cand);
+            if (items >= 8.0 * resident) cx = cand;
+        }
+        if (cx == g.nx) {
+            for (int cand : cands)
+                if (cand < g.nx && (double)tiles * ((g.nx + cand - 1) / cand) >= 2.0 * resident) cx = cand;
+        }
+        c->fused_cx = cx;
+    }
+    if (st->items_cx != cx || st->items_t != p.t || !st->d_items) {
+        std::vector<int4> items = fused_items(g, TY, TZ, cx, p.t);
+        cudaFree(st->d_items);
+        st->d_items = nullptr;
+        PC_CUDA_CHECK(cudaMalloc(&st->d_items, items.size() * sizeof(int4)));
+        PC_CUDA_CHECK(cudaMemcpy(st->d_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+        st->n_items = (int)items.size();
+        st->items_cx = cx;
+        st->items_t = p.t;
+    }
+    dim3 blk(TZ, TY / 2 + 1);
+    kern<<<st->n_items, blk, smem, s>>>(a, p, st->d_items, maps);
+    PC_CUDA_CHECK(cudaGetLastError());
+    return PC_OK;
 }
 
 template <typename T, int TY, int TZ, int S>
@@ -316,68 +581,39 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
     FusedState* st = state_of(c);
     bool same = st->ready;
     for (int q = 0; q < 6 && same; ++q) same = st->key_f[0][q] == c->F[0][q] && st->key_f[1][q] == c->F[1][q];
-    for (int q = 0; q < 3 && same; ++q) same = st->key_cb[q] == c->cb[q];
     if (!same) {
         for (int set = 0; set < 2; ++set)
             for (int q = 0; q < 3; ++q) {
                 int rc = make_map(&st->maps[set].e[q], c->F[set][q], g, G::EW, G::EH);
                 if (!rc) rc = make_map(&st->maps[set].h[q], c->F[set][3 + q], g, G::HW, G::HH);
-                if (!rc) rc = make_map(&st->maps[set].cb[q], c->cb[q], g, G::CW, G::CH);
                 if (rc) return rc;
             }
         for (int q = 0; q < 6; ++q) {
             st->key_f[0][q] = c->F[0][q];
             st->key_f[1][q] = c->F[1][q];
         }
-        for (int q = 0; q < 3; ++q) st->key_cb[q] = c->cb[q];
         st->ready = true;
     }
     const int in = c->cur, out = c->cur ^ 1;
     FieldArgs<T> a = make_field_args<T>(c, in, out);
     CpmlArgs<T> p = make_cpml_args<T>(c, in, out);
-    constexpr int smem = fused_smem_bytes<T, TY, TZ, S>();
-    static bool attr_set[2] = {false, false};
-    auto kern_cp = fused3<T, TY, TZ, S, true>;
-    auto kern_nc = fused3<T, TY, TZ, S, false>;
-    if (!attr_set[sizeof(T) == 8]) {
-        PC_CUDA_CHECK(cudaFuncSetAttribute(kern_cp, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        PC_CUDA_CHECK(cudaFuncSetAttribute(kern_nc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        attr_set[sizeof(T) == 8] = true;
+    if (p.t > 0 && p.total >= ((int64_t)1 << 31)) return launch_split_step(c, s);  // 32-bit psi offsets
+    const int smem = fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * PC_MAX_CPML * (int)sizeof(T);
+    const bool cp = p.t > 0, hc = a.da[0] != nullptr, ca = a.ca[0] != nullptr;
+    const FusedMaps& m = st->maps[in];
+    int rc;
+    const int key = (cp ? 4 : 0) | (hc ? 2 : 0) | (ca ? 1 : 0);
+    switch (key) {
+        case 0: rc = launch_variant<T, TY, TZ, S, false, false, false>(c, s, a, p, m, smem, st); break;
+        case 1: rc = launch_variant<T, TY, TZ, S, false, false, true>(c, s, a, p, m, smem, st); break;
+        case 2: rc = launch_variant<T, TY, TZ, S, false, true, false>(c, s, a, p, m, smem, st); break;
+        case 3: rc = launch_variant<T, TY, TZ, S, false, true, true>(c, s, a, p, m, smem, st); break;
+        case 4: rc = launch_variant<T, TY, TZ, S, true, false, false>(c, s, a, p, m, smem, st); break;
+        case 5: rc = launch_variant<T, TY, TZ, S, true, false, true>(c, s, a, p, m, smem, st); break;
+        case 6: rc = launch_variant<T, TY, TZ, S, true, true, false>(c, s, a, p, m, smem, st); break;
+        default: rc = launch_variant<T, TY, TZ, S, true, true, true>(c, s, a, p, m, smem, st); break;
     }
-    int cx = c->fused_cx;
-    if (cx <= 0) {
-        int sms = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
-        if (sms <= 0) sms = 152;
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern_cp, TY * TZ, smem);
-        if (per_sm <= 0) per_sm = 1;
-        const int resident = sms * per_sm;
-        const int tiles = ((g.nz + TZ - 1) / TZ) * ((g.ny + TY - 1) / TY);
-        // cost model: waves x planes streamed per CTA (chunk + 2 pipeline planes)
-        const int cands[] = {8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512};
-        double best = 1e300;
-        cx = g.nx;
-        for (int cand : cands) {
-            if (cand > g.nx) break;
-            const int chunks = (g.nx + cand - 1) / cand;
-            const double ctas = (double)tiles * chunks;
-            const double waves = ctas / resident;
-            const double cost = (waves < 1.0 ? 1.0 : waves) * (cand + 2);
-            if (cost < best * 0.97) {
-                best = cost;
-                cx = cand;
-            }
-        }
-        c->fused_cx = cx;
-    }
-    dim3 blk(TZ, TY);
-    dim3 grd((g.nz + TZ - 1) / TZ, (g.ny + TY - 1) / TY, (g.nx + cx - 1) / cx);
-    if (p.t > 0)
-        kern_cp<<<grd, blk, smem, s>>>(a, p, cx, st->maps[in]);
-    else
-        kern_nc<<<grd, blk, smem, s>>>(a, p, cx, st->maps[in]);
-    PC_CUDA_CHECK(cudaGetLastError());
+    if (rc) return rc;
     ++c->launches;
     c->cur = out;
     return PC_OK;
@@ -387,11 +623,12 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
 
 int launch_fused_step(pc_ctx* c, cudaStream_t s) {
     if (c->g.ndim != 3) return launch_split_step(c, s);
-    if (c->g.precision == 8) return fused_t<double, 8, 32, 3>(c, s);
-    return fused_t<float, 8, 32, 6>(c, s);
+    if (c->g.precision == 8) return fused_t<double, 16, 32, 3>(c, s);
+    return fused_t<float, 16, 32, 5>(c, s);
 }
 
 void destroy_fused_state(pc_ctx* c) {
+    if (c->fused_state) cudaFree(static_cast<FusedState*>(c->fused_state)->d_items);
     delete static_cast<FusedState*>(c->fused_state);
     c->fused_state = nullptr;
 }

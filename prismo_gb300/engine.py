@@ -239,6 +239,8 @@ class FDTDEngine:
 
     def check_status(self):
         st = self.status()
+        if st & _lib.PC_STATUS_BOUNDS:
+            raise IndexError("a kernel computed an out-of-range auxiliary-array offset (skipped)")
         if st & _lib.PC_STATUS_TIMEOUT:
             raise TimeoutError("a bounded device wait ran out inside the FDTD kernel")
         if st & _lib.PC_STATUS_NONFINITE:
@@ -254,6 +256,76 @@ class FDTDEngine:
         n = C.c_int64(0)
         _lib.check(self.lib.pc_profile_read(self.ctx, C.byref(ms), C.byref(n)), "pc_profile_read")
         return float(ms.value), int(n.value)
+
+    # -- autotuning ---------------------------------------------------------------
+    def autotune(self, candidates=(8, 16, 24, 32, 48, 64, 96), steps: int = 6, cache: bool = True):
+        """Pick the x-chunk length of the fused 3D schedule by timing a few steps of
+        each candidate with CUDA events; the fields and psi are restored afterwards.
+        Results are cached per (dims, CPML thickness, precision) in
+        ``$PRISMO_GB300_CACHE`` (default ~/.cache/prismo_gb300/tune.json)."""
+        import json
+        import os
+
+        torch = _torch()
+        if self.is_2d or not self.pingpong:
+            return None
+        key = f"{self.dims}|t={0 if self.pml is None else self.pml.thickness}|{self.precision}|" \
+              f"{torch.cuda.get_device_name(self.device)}"
+        path = os.environ.get("PRISMO_GB300_CACHE", os.path.join(os.path.expanduser("~"), ".cache",
+                                                                 "prismo_gb300", "tune.json"))
+        table = {}
+        if cache and os.path.exists(path):
+            try:
+                with open(path) as f:
+                    table = json.load(f)
+            except (OSError, ValueError):
+                table = {}
+        if cache and key in table:
+            self.set_chunk(int(table[key]))
+            return int(table[key])
+        saved_sets = [t.clone() for t in self.sets]
+        saved_psi = [t.clone() for t in self.psi]
+        saved_cur = self.cur
+        best, best_ms = None, float("inf")
+        nsrc = len(self.sources)
+        amps = np.zeros((steps, nsrc)) if nsrc else None
+        for cx in candidates:
+            if cx >= self.dims[0]:
+                continue
+            self.set_chunk(cx)
+            self.step(2, None if amps is None else amps[:2])
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(self.stream)
+            self.step(steps, amps)
+            e1.record(self.stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            if ms < best_ms:
+                best, best_ms = cx, ms
+        for dst, src in zip(self.sets, saved_sets):
+            dst.copy_(src)
+        for dst, src in zip(self.psi, saved_psi):
+            dst.copy_(src)
+        _lib.check(self.lib.pc_set_current_set(self.ctx, saved_cur), "pc_set_current_set")
+        self.check_status()
+        if best is not None:
+            self.set_chunk(best)
+            if cache:
+                table[key] = best
+                try:
+                    os.makedirs(os.path.dirname(path), exist_ok=True)
+                    with open(path, "w") as f:
+                        json.dump(table, f, indent=1)
+                except OSError:
+                    pass
+        return best
+
+    def set_chunk(self, cx: int):
+        _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_FUSED_CHUNK, int(cx)), "pc_set_tuning")
+
+    def chunk(self) -> int:
+        return int(self.lib.pc_get_tuning(self.ctx, _lib.PC_TUNE_FUSED_CHUNK))
 
     def launch_count(self) -> int:
         return int(self.lib.pc_launch_count(self.ctx))

@@ -131,6 +131,7 @@ def test_corrected_2d_matches_oracle(torch, lossy, cpml):
         load_fields(eng, init, torch)
         eng.step(nsteps)
         out = read_fields(eng)
+        assert eng.check_status() == 0
         for c in COMPS:
             ref = o.F[c]
             if prec == "fp64":
@@ -153,6 +154,7 @@ def test_fused_equals_split_fp32_long_run(torch):
         load_fields(eng, init, torch)
         eng.step(101)
         outs.append(read_fields(eng))
+        assert eng.check_status() == 0
         eng.close()
     for c in COMPS:
         assert rel_l2(outs[1][c], outs[0][c]) <= 1e-6, c
@@ -178,7 +180,33 @@ def test_point_source_matches_oracle(torch):
         t = np.cumsum(np.full(n, dt))
         eng.step(n, np.array([wf(x) for x in t])[:, None])
         out = read_fields(eng)
+        assert eng.check_status() == 0
         for c in COMPS:
             tol = 1e-12 if prec == "fp64" else 1e-5
             assert rel_l2(out[c], o.F[c]) <= tol, (prec, c, rel_l2(out[c], o.F[c]))
         eng.close()
+
+
+@pytest.mark.parametrize("chunk", [0, 5, 7])
+def test_fused_chunking_with_cpml_slabs(torch, chunk):
+    """x-chunks of every length end on the last plane with y/z CPML slabs active."""
+    from prismo_gb300 import _lib
+    from prismo_gb300.pml import PMLParams
+
+    g, mats, init = _random_case((29, 35, 41), False, seed=9, lossy=False)
+    dt = g.suggest_dt(0.5)
+    o = O.OracleFDTD(g, dt, mats, cpml_layers=5)
+    for c in COMPS:
+        o.F[c][...] = init[c]
+    o.run(12)
+    eng = make_engine(g.dims, g.spacing, dt, False, precision="fp32", sched="fused", material_arrays=mats,
+                      pml=PMLParams(thickness=5))
+    if chunk:
+        _lib.check(eng.lib.pc_set_tuning(eng.ctx, _lib.PC_TUNE_FUSED_CHUNK, chunk))
+    load_fields(eng, init, torch)
+    eng.step(12)
+    out = read_fields(eng)
+    assert eng.check_status() == 0
+    for c in COMPS:
+        assert rel_l2(out[c], o.F[c]) <= 1e-5, c
+    eng.close()
