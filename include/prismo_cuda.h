@@ -141,6 +141,30 @@ int64_t pc_get_tuning(const pc_ctx* ctx, int32_t key);
 int pc_profile(pc_ctx* ctx, int32_t enable);
 int pc_profile_read(pc_ctx* ctx, double* total_ms, int64_t* count);
 
+/* Allocation-free stepping.  This entry point has no counterpart in the
+ * reference; it serves callers that may not allocate device memory: a host
+ * application whose device memory is owned entirely by its own pool allocator,
+ * or a time loop that must not pay cudaMalloc's latency and device-wide
+ * synchronisation.  It runs nsteps of the fused 3D corrected stepper (float32 or
+ * float64, vacuum mu, sigma = 0, no CPML and no sources) without a context and
+ * without allocating: the caller passes both field sets (set0/set1, six device
+ * pointers each, padded layout of this header) and the three Cb arrays; `cur`
+ * names the set holding the current fields; the return value is the set that
+ * holds the result (>= 0) or a PC_ERR_* code.
+ *   - Scratch (the kernel's work-item list and its status word) lives in one
+ *     fixed device array of 32768 work items (about 512 KB) that every GPU
+ *     loading the library keeps until the process exits.  Grids needing more
+ *     work items (more than 32768 tiles of 16 x 32 cells times x-chunks) are
+ *     rejected with PC_ERR_INVALID.
+ *   - The first call on a device resolves that array's device address (call it
+ *     with that device current, and before any stream capture).
+ *   - Every call shares the array and resets the status word at its start;
+ *     calls that overlap on the GPU race.
+ *   - status_out (host, nullable) receives the PC_STATUS_* bits; passing it
+ *     synchronises the stream. */
+int pc_fused_steps_noalloc(const pc_grid_desc* desc, void* const set0[6], void* const set1[6], int32_t cur,
+                           const void* const cb[3], int32_t nsteps, void* stream, uint32_t* status_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -76,6 +76,8 @@ SIGNATURES = {
     "pc_launch_count": (C.c_int64, [C.c_void_p]),
     "pc_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),
     "pc_get_tuning": (C.c_int64, [C.c_void_p, C.c_int32]),
+    "pc_fused_steps_noalloc": (C.c_int, [C.POINTER(GridDesc), VPP, VPP, C.c_int32, VPP, C.c_int32, C.c_void_p,
+                                         C.POINTER(C.c_uint32)]),
     "pc_profile": (C.c_int, [C.c_void_p, C.c_int32]),
     "pc_profile_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
 }

@@ -619,6 +619,144 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
     return PC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free stepping (pc_fused_steps_noalloc)
+//
+// The fused kernel reads its work items from global memory and reports
+// non-finite values through a status word.  Callers that may not allocate device
+// memory get both from this fixed file-scope array instead: PC_NOALLOC_MAX_ITEMS
+// work items followed by one status word (about 512 KB, held by every device that
+// loads the library until the process exits).  All calls share it.
+// ---------------------------------------------------------------------------
+#define PC_NOALLOC_MAX_ITEMS 32768
+static __device__ __align__(256) int4 g_noalloc_scratch[PC_NOALLOC_MAX_ITEMS + 1];
+
+// uniform (k-tile, j-tile, chunk) work items, all of equal cost without CPML
+__global__ void noalloc_fill_items(int4* items, int ntk, int ntj, int nchunks, int cx, int nx, int TZ_, int TY_,
+                                   uint32_t* status) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b == 0) *status = 0u;
+    const int n = ntk * ntj * nchunks;
+    if (b >= n) return;
+    const int kt = b % ntk, jt = (b / ntk) % ntj, ch = b / (ntk * ntj);
+    const int ib = ch * cx;
+    items[b] = make_int4(kt * TZ_, jt * TY_, ib, min(nx, ib + cx));
+}
+
+}  // namespace
+
+namespace {
+int g_noalloc_ready[128];
+int4* g_noalloc_ptr[128];
+
+template <typename T>
+int noalloc_run(const pc_grid_desc& g, void* const set0[6], void* const set1[6], int cur, const void* const cb[3],
+                int nsteps, cudaStream_t s, int4* scratch) {
+    constexpr int TY = 16, TZ = 32, S = (sizeof(T) == 4) ? 5 : 3;
+    using G = FusedGeom<T, TY, TZ>;
+    auto kern = fused3<T, TY, TZ, S, false, false, false>;
+    const int smem = fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * PC_MAX_CPML * (int)sizeof(T);
+    PC_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    const int ntk = (g.nz + TZ - 1) / TZ, ntj = (g.ny + TY - 1) / TY;
+    // x-chunk: about 8 work items per resident CTA, within the scratch capacity
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TZ * (TY / 2 + 1), smem);
+    const double want = 8.0 * (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
+    int cx = g.nx;
+    const int cands[] = {16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512};
+    for (int cand : cands)
+        if (cand < g.nx && (double)ntk * ntj * ((g.nx + cand - 1) / cand) >= want) cx = cand;
+    int nchunks = (g.nx + cx - 1) / cx;
+    while ((int64_t)ntk * ntj * nchunks > PC_NOALLOC_MAX_ITEMS && cx < g.nx) {
+        cx *= 2;
+        nchunks = (g.nx + cx - 1) / cx;
+    }
+    const int nitems = ntk * ntj * nchunks;
+    if (nitems > PC_NOALLOC_MAX_ITEMS) return PC_ERR_INVALID;  // grid beyond the fixed scratch
+    FusedMaps maps[2];
+    for (int set = 0; set < 2; ++set) {
+        void* const* F = set == 0 ? set0 : set1;
+        for (int q = 0; q < 3; ++q) {
+            int rc = make_map(&maps[set].e[q], F[q], g, G::EW, G::EH);
+            if (!rc) rc = make_map(&maps[set].h[q], F[3 + q], g, G::HW, G::HH);
+            if (rc) return rc;
+        }
+    }
+    int4* items = scratch;
+    uint32_t* status = reinterpret_cast<uint32_t*>(scratch + PC_NOALLOC_MAX_ITEMS);
+    noalloc_fill_items<<<(nitems + 255) / 256, 256, 0, s>>>(items, ntk, ntj, nchunks, cx, g.nx, TZ, TY, status);
+    PC_CUDA_CHECK(cudaGetLastError());
+    FieldArgs<T> a{};
+    a.nx = g.nx;
+    a.ny = g.ny;
+    a.nz = g.nz;
+    a.pitch = g.pitch;
+    a.dx = T(g.dx);
+    a.dy = T(g.dy);
+    a.dz = T(g.dz);
+    a.inv_dx = T(1.0 / g.dx);
+    a.inv_dy = T(1.0 / g.dy);
+    a.inv_dz = T(1.0 / g.dz);
+    a.da_s = T(1.0);
+    a.db_s = T((g.dt / (4.0 * M_PI * 1e-7 * 1.0)) / (1.0 + 0.0));  // vacuum mu: dt / mu0
+    a.status = status;
+    for (int q = 0; q < 3; ++q) a.cb[q] = static_cast<const T*>(cb[q]);
+    CpmlArgs<T> pm{};
+    for (int n = 0; n < nsteps; ++n) {
+        void* const* Fi = cur == 0 ? set0 : set1;
+        void* const* Fo = cur == 0 ? set1 : set0;
+        for (int q = 0; q < 3; ++q) {
+            a.Ein[q] = static_cast<const T*>(Fi[q]);
+            a.Hin[q] = static_cast<const T*>(Fi[3 + q]);
+            a.Eout[q] = static_cast<T*>(Fo[q]);
+            a.Hout[q] = static_cast<T*>(Fo[3 + q]);
+        }
+        kern<<<nitems, dim3(TZ, TY / 2 + 1), smem, s>>>(a, pm, items, maps[cur]);
+        PC_CUDA_CHECK(cudaGetLastError());
+        cur ^= 1;
+    }
+    return cur;
+}
+}  // namespace
+
+extern "C" int pc_fused_steps_noalloc(const pc_grid_desc* d, void* const set0[6], void* const set1[6],
+                                      int32_t cur, const void* const cb[3], int32_t nsteps, void* stream,
+                                      uint32_t* status_out) {
+    if (!d || !set0 || !set1 || !cb || nsteps < 0 || (cur != 0 && cur != 1)) return PC_ERR_INVALID;
+    if (d->ndim != 3 || d->mode != PC_MODE_CORRECTED || (d->precision != 4 && d->precision != 8))
+        return PC_ERR_INVALID;
+    if (d->nx < 3 || d->ny < 3 || d->nz < 3 || d->pitch < d->nz || d->pitch % 32 != 0) return PC_ERR_INVALID;
+    if (!(d->dt > 0) || !(d->dx > 0) || !(d->dy > 0) || !(d->dz > 0)) return PC_ERR_INVALID;
+    for (int q = 0; q < 6; ++q)
+        if (!set0[q] || !set1[q]) return PC_ERR_INVALID;
+    for (int q = 0; q < 3; ++q)
+        if (!cb[q]) return PC_ERR_INVALID;
+    int dev = 0;
+    PC_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) return PC_ERR_INVALID;
+    if (!g_noalloc_ready[dev]) {
+        // first call on this device (the device is current): resolve the device
+        // address of the scratch array; host code may not use the symbol itself
+        void* ptr = nullptr;
+        PC_CUDA_CHECK(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = static_cast<int4*>(ptr);
+        g_noalloc_ready[dev] = 1;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    const int rc = d->precision == 8
+                       ? noalloc_run<double>(*d, set0, set1, cur, cb, nsteps, s, g_noalloc_ptr[dev])
+                       : noalloc_run<float>(*d, set0, set1, cur, cb, nsteps, s, g_noalloc_ptr[dev]);
+    if (rc < 0) return rc;
+    if (status_out) {
+        PC_CUDA_CHECK(cudaMemcpyAsync(status_out, g_noalloc_ptr[dev] + PC_NOALLOC_MAX_ITEMS, sizeof(uint32_t),
+                                      cudaMemcpyDeviceToHost, s));
+        PC_CUDA_CHECK(cudaStreamSynchronize(s));
+    }
+    return rc;
+}
+
+namespace {
 }  // namespace
 
 int launch_fused_step(pc_ctx* c, cudaStream_t s) {
