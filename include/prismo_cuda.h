@@ -122,6 +122,39 @@ int pc_add_source(pc_ctx* ctx, int32_t comp, const int64_t* offsets, const doubl
  * there are no sources). */
 int pc_step(pc_ctx* ctx, int32_t nsteps, const double* amps, void* stream);
 
+/* Dispersive (ADE) region: E components whose own index lies in
+ * [box0,box1) x [box2,box3) x [box4,box5) use the auxiliary-differential-equation
+ * update instead of Ca/Cb (materials/ade.py:100-160 recursions with the
+ * coefficients of materials/dispersion.py:189-336, coupled to E through the
+ * polarisation current):
+ *   Lorentz (kind 0): P+ = C0 E+ + C1 E + C2 P + C3 P-       (aux: P, P-)
+ *   Drude   (kind 1): J+ = C1 J + C0 (E+ + E)/2               (aux: J)
+ *   Debye   (kind 2): P+ = C1 P + C0 (E+ + E)/2               (aux: P)
+ * with eps_inf (E+ - E) + sum dP (or dt J terms) = (dt/eps0) curl H, solved for E+.
+ * aux[c][p][0..1]: caller-owned zeroed device arrays over the box (C order,
+ * float context precision), per E component c and pole p. */
+typedef struct pc_ade_region {
+    int32_t box[6];
+    int32_t npoles;
+    int32_t kind[4];
+    double eps_inf;
+    double c0[4], c1[4], c2[4], c3[4];
+    void* aux[3][4][2];
+} pc_ade_region;
+
+int pc_set_ade(pc_ctx* ctx, int32_t nregions, const pc_ade_region* regions, double eps0);
+
+/* DFT monitor (monitors/field.py:138-143, monitors/dft.py:108-137): after every
+ * step (and after the sources) F_f += field(t_{n+1}) exp(-i omega_f t_{n+1}) dt at
+ * the npts element offsets of component comp.  t0 is t_{n+1} of the next step.
+ * d_acc is caller-owned float [nf][npts][4] = (sum re, sum im, Kahan compensation
+ * re, im), zeroed; the estimate is sum - compensation.  Samples are batched (16
+ * steps) and folded in with a float64 phase recurrence; call pc_dft_flush before
+ * reading d_acc.  Returns the monitor id. */
+int pc_add_dft(pc_ctx* ctx, int32_t comp, const int64_t* offsets, int32_t npts, const double* omega,
+               int32_t nf, double dt, double t0, void* d_acc);
+int pc_dft_flush(pc_ctx* ctx, int32_t id, void* stream);
+
 /* Read and clear the device status word (PC_STATUS_* bits). Synchronises the
  * stream. */
 int pc_status(pc_ctx* ctx, uint32_t* flags, void* stream);

@@ -51,6 +51,20 @@ class GridDesc(C.Structure):
     ]
 
 
+class AdeRegion(C.Structure):
+    _fields_ = [
+        ("box", C.c_int32 * 6),
+        ("npoles", C.c_int32),
+        ("kind", C.c_int32 * 4),
+        ("eps_inf", C.c_double),
+        ("c0", C.c_double * 4),
+        ("c1", C.c_double * 4),
+        ("c2", C.c_double * 4),
+        ("c3", C.c_double * 4),
+        ("aux", ((C.c_void_p * 2) * 4) * 3),
+    ]
+
+
 P6 = C.c_void_p * 6
 P3 = C.c_void_p * 3
 D3 = C.POINTER(C.c_double) * 3
@@ -72,6 +86,10 @@ SIGNATURES = {
     "pc_set_cpml": (C.c_int, [C.c_void_p, C.c_int32, DPP, DPP, DPP, C.c_void_p, C.c_void_p]),
     "pc_add_source": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.c_int32]),
     "pc_step": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_void_p]),
+    "pc_set_ade": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(AdeRegion), C.c_double]),
+    "pc_add_dft": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_double),
+                             C.c_int32, C.c_double, C.c_double, C.c_void_p]),
+    "pc_dft_flush": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "pc_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p]),
     "pc_launch_count": (C.c_int64, [C.c_void_p]),
     "pc_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),

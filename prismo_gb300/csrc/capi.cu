@@ -2,6 +2,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <math.h>
+
 #include <new>
 #include <vector>
 
@@ -89,6 +91,13 @@ void pc_destroy(pc_ctx* c) {
     for (auto& s : c->sources) {
         cudaFree(s.d_off);
         cudaFree(s.d_w);
+    }
+    for (auto& m : c->dfts) {
+        cudaFree(m.d_off);
+        cudaFree(m.d_ring);
+        cudaFree(m.d_table);
+        cudaFree(m.d_state);
+        cudaFree(m.d_rot);
     }
     cudaFree(c->d_amps);
     cudaFree(c->d_cpml_coef);
@@ -282,7 +291,7 @@ int pc_step(pc_ctx* c, int32_t nsteps, const double* amps, void* stream) {
         }
         if (c->g.mode == PC_MODE_LEGACY)
             rc = launch_legacy_step(c, s);
-        else if (c->g.sched == PC_SCHED_FUSED)
+        else if (c->g.sched == PC_SCHED_FUSED && c->ade_n == 0)
             rc = launch_fused_step(c, s);
         else
             rc = launch_split_step(c, s);
@@ -290,8 +299,97 @@ int pc_step(pc_ctx* c, int32_t nsteps, const double* amps, void* stream) {
         if (ev1) PC_CUDA_CHECK(cudaEventRecord(ev1, s));
         rc = launch_sources(c, n, s);
         if (rc) return rc;
+        if (!c->dfts.empty()) {
+            rc = dft_after_step(c, s);
+            if (rc) return rc;
+        }
     }
     return PC_OK;
+}
+
+int pc_add_dft(pc_ctx* c, int32_t comp, const int64_t* offsets, int32_t npts, const double* omega, int32_t nf,
+               double dt, double t0, void* d_acc) {
+    if (!c || comp < 0 || comp > 5 || npts <= 0 || !offsets || !omega || nf <= 0 || !(dt > 0) || !d_acc)
+        return PC_ERR_INVALID;
+    const int64_t lim = (int64_t)c->g.nx * c->g.ny * c->g.pitch;
+    for (int i = 0; i < npts; ++i)
+        if (offsets[i] < 0 || offsets[i] >= lim) return PC_ERR_INVALID;
+    DftMonitor m{};
+    m.comp = comp;
+    m.npts = npts;
+    m.nf = nf;
+    m.T = 16;
+    m.dt = dt;
+    m.d_acc = static_cast<float4*>(d_acc);
+    std::vector<double> st(2 * nf), rot(2 * nf);
+    for (int f = 0; f < nf; ++f) {
+        // phase of the first sample, t0 = t_{n+1} of the next step, and one-step rotation
+        st[2 * f] = cos(-omega[f] * t0);
+        st[2 * f + 1] = sin(-omega[f] * t0);
+        rot[2 * f] = cos(-omega[f] * dt);
+        rot[2 * f + 1] = sin(-omega[f] * dt);
+    }
+    bool ok = cudaMalloc(&m.d_off, npts * sizeof(int64_t)) == cudaSuccess &&
+              cudaMalloc(&m.d_ring, (size_t)m.T * npts * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&m.d_table, (size_t)m.T * nf * sizeof(float2)) == cudaSuccess &&
+              cudaMalloc(&m.d_state, nf * sizeof(double2)) == cudaSuccess &&
+              cudaMalloc(&m.d_rot, nf * sizeof(double2)) == cudaSuccess;
+    ok = ok && cudaMemcpy(m.d_off, offsets, npts * sizeof(int64_t), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(m.d_state, st.data(), nf * sizeof(double2), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(m.d_rot, rot.data(), nf * sizeof(double2), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (!ok) {
+        cudaFree(m.d_off);
+        cudaFree(m.d_ring);
+        cudaFree(m.d_table);
+        cudaFree(m.d_state);
+        cudaFree(m.d_rot);
+        return PC_ERR_CUDA;
+    }
+    c->dfts.push_back(m);
+    return (int)c->dfts.size() - 1;
+}
+
+int pc_set_ade(pc_ctx* c, int32_t n, const pc_ade_region* regs, double eps0) {
+    if (!c || n < 0 || n > PC_MAX_ADE_REGIONS || (n > 0 && !regs) || !(eps0 > 0)) return PC_ERR_INVALID;
+    if (n > 0 && c->g.mode == PC_MODE_LEGACY) return PC_ERR_INVALID;  // no ADE coupling in the reference
+    const double dt = c->g.dt;
+    for (int r = 0; r < n; ++r) {
+        const pc_ade_region& R = regs[r];
+        if (R.npoles < 0 || R.npoles > PC_MAX_ADE_POLES) return PC_ERR_INVALID;
+        for (int a = 0; a < 3; ++a)
+            if (R.box[2 * a] < 0 || R.box[2 * a + 1] < R.box[2 * a]) return PC_ERR_INVALID;
+        // E+ = (ce E + S - sum aux) / den   (see the oracle's ade_e_coefficients)
+        double den = R.eps_inf, ce = R.eps_inf;
+        for (int p = 0; p < R.npoles; ++p) {
+            if (R.kind[p] == 0) {
+                den += R.c0[p];
+                ce -= R.c1[p];
+            } else if (R.kind[p] == 1) {
+                den += dt * R.c0[p] / 4.0;
+                ce -= dt * R.c0[p] / 4.0;
+            } else if (R.kind[p] == 2) {
+                den += R.c0[p] / 2.0;
+                ce -= R.c0[p] / 2.0;
+            } else {
+                return PC_ERR_INVALID;
+            }
+            for (int comp = 0; comp < 3; ++comp) {
+                if (!R.aux[comp][p][0]) return PC_ERR_INVALID;
+                if (R.kind[p] == 0 && !R.aux[comp][p][1]) return PC_ERR_INVALID;
+            }
+        }
+        c->ade[r] = R;
+        c->ade_ce[r] = ce / den;
+        c->ade_inv[r] = 1.0 / den;
+    }
+    c->ade_n = n;
+    c->ade_sdt = dt / eps0;
+    return PC_OK;
+}
+
+int pc_dft_flush(pc_ctx* c, int32_t id, void* stream) {
+    if (!c || id < 0 || id >= (int)c->dfts.size()) return PC_ERR_INVALID;
+    return dft_flush_monitor(c, c->dfts[id], (cudaStream_t)stream);
 }
 
 int pc_status(pc_ctx* c, uint32_t* flags, void* stream) {

@@ -26,6 +26,38 @@ struct SourceDesc {
     double* d_w;      // device weights (float64, converted in-kernel)
 };
 
+// One DFT monitor: samples of `comp` at `npts` element offsets, accumulated for
+// `nf` frequencies (see dft.cu).
+struct DftMonitor {
+    int comp, npts, nf, T, rows;
+    double dt;
+    int64_t* d_off;   // [npts] element offsets (ctx-owned)
+    float* d_ring;    // [T][npts] samples of the pending batch (ctx-owned)
+    float2* d_table;  // [T][nf] float32 phases of the batch (ctx-owned)
+    double2* d_state; // [nf] float64 phase of the next sample (ctx-owned)
+    double2* d_rot;   // [nf] exp(-i w dt) (ctx-owned)
+    float4* d_acc;    // [nf][npts] (sum re, sum im, comp re, comp im), caller-owned
+};
+
+#define PC_MAX_ADE_REGIONS 2
+#define PC_MAX_ADE_POLES 4
+
+// Device view of the dispersive regions (see pc_ade_region in the header).
+template <typename T>
+struct AdeArgs {
+    int nreg;
+    int box[PC_MAX_ADE_REGIONS][6];
+    int npoles[PC_MAX_ADE_REGIONS];
+    int kind[PC_MAX_ADE_REGIONS][PC_MAX_ADE_POLES];
+    T ce[PC_MAX_ADE_REGIONS];   // coefficient of E^n
+    T inv[PC_MAX_ADE_REGIONS];  // 1 / denominator
+    T sdt;                       // dt / eps0 (curl -> S)
+    T dt;
+    T c0[PC_MAX_ADE_REGIONS][PC_MAX_ADE_POLES], c1[PC_MAX_ADE_REGIONS][PC_MAX_ADE_POLES];
+    T c2[PC_MAX_ADE_REGIONS][PC_MAX_ADE_POLES], c3[PC_MAX_ADE_REGIONS][PC_MAX_ADE_POLES];
+    T* aux[PC_MAX_ADE_REGIONS][3][PC_MAX_ADE_POLES][2];
+};
+
 // Geometry of the slab-only psi storage.  Axis a keeps four slots; the lower
 // slab index s = idx (idx < t), the upper s = idx - (n - 2t) (idx >= n - t).
 struct PsiLayout {
@@ -87,8 +119,13 @@ struct pc_ctx {
     void* psi[2];
     void* d_cpml_coef;  // [3 axes][b, a, kinv][n_axis] in context precision
     void* d_cpml_slab;  // [3 axes][b, a, kinv][2t]: the same values at slab indices only
-    // sources
+    // dispersive regions (host copy, converted per launch)
+    int ade_n;
+    pc_ade_region ade[PC_MAX_ADE_REGIONS];
+    double ade_ce[PC_MAX_ADE_REGIONS], ade_inv[PC_MAX_ADE_REGIONS], ade_sdt;
+    // sources and DFT monitors
     std::vector<pc::SourceDesc> sources;
+    std::vector<pc::DftMonitor> dfts;
     double* d_amps;
     size_t amps_cap;
     // fused schedule: cached tensor maps and the chosen x-chunk length
@@ -117,6 +154,8 @@ int launch_split_step(pc_ctx* c, cudaStream_t s);
 int launch_sources(pc_ctx* c, int step_in_batch, cudaStream_t s);
 int launch_fused_step(pc_ctx* c, cudaStream_t s);
 void destroy_fused_state(pc_ctx* c);
+int dft_after_step(pc_ctx* c, cudaStream_t s);
+int dft_flush_monitor(pc_ctx* c, DftMonitor& m, cudaStream_t s);
 
 }  // namespace pc
 

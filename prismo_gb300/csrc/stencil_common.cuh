@@ -73,6 +73,71 @@ __device__ __forceinline__ T cpml2(const CpmlArgs<T>& p, int slot, const Idx2& q
 }
 
 template <typename T>
+static AdeArgs<T> make_ade_args(pc_ctx* c) {
+    AdeArgs<T> A{};
+    A.nreg = c->ade_n;
+    A.sdt = T(c->ade_sdt);
+    A.dt = T(c->g.dt);
+    for (int r = 0; r < c->ade_n; ++r) {
+        const pc_ade_region& R = c->ade[r];
+        for (int q = 0; q < 6; ++q) A.box[r][q] = R.box[q];
+        A.npoles[r] = R.npoles;
+        A.ce[r] = T(c->ade_ce[r]);
+        A.inv[r] = T(c->ade_inv[r]);
+        for (int p = 0; p < R.npoles; ++p) {
+            A.kind[r][p] = R.kind[p];
+            A.c0[r][p] = T(R.c0[p]);
+            A.c1[r][p] = T(R.c1[p]);
+            A.c2[r][p] = T(R.c2[p]);
+            A.c3[r][p] = T(R.c3[p]);
+            for (int comp = 0; comp < 3; ++comp)
+                for (int w = 0; w < 2; ++w) A.aux[r][comp][p][w] = static_cast<T*>(R.aux[comp][p][w]);
+        }
+    }
+    return A;
+}
+
+// ADE update of one E component at (i, j, k) given E^n and the (CPML-modified)
+// curl; returns true and E^{n+1} in e when the point lies in a dispersive region.
+template <typename T>
+__device__ __forceinline__ bool ade_update(const AdeArgs<T>& A, int comp, int i, int j, int k, T curl, T& e) {
+    for (int r = 0; r < A.nreg; ++r) {
+        const int* b = A.box[r];
+        if (i < b[0] || i >= b[1] || j < b[2] || j >= b[3] || k < b[4] || k >= b[5]) continue;
+        const int64_t o = ((int64_t)(i - b[0]) * (b[3] - b[2]) + (j - b[2])) * (b[5] - b[4]) + (k - b[4]);
+        const T e0 = e;
+        T acc = A.ce[r] * e0 + A.inv[r] * (A.sdt * curl);
+        for (int p = 0; p < A.npoles[r]; ++p) {
+            const T a0 = A.aux[r][comp][p][0][o];
+            if (A.kind[r][p] == 0) {
+                const T a1 = A.aux[r][comp][p][1][o];
+                acc -= A.inv[r] * ((A.c2[r][p] - T(1)) * a0 + A.c3[r][p] * a1);
+            } else if (A.kind[r][p] == 1) {
+                acc -= A.inv[r] * (T(0.5) * A.dt * (T(1) + A.c1[r][p]) * a0);
+            } else {
+                acc -= A.inv[r] * ((A.c1[r][p] - T(1)) * a0);
+            }
+        }
+        const T e1 = acc;
+        for (int p = 0; p < A.npoles[r]; ++p) {
+            T* x0 = A.aux[r][comp][p][0];
+            const T a0 = x0[o];
+            if (A.kind[r][p] == 0) {
+                T* x1 = A.aux[r][comp][p][1];
+                const T pn = A.c0[r][p] * e1 + A.c1[r][p] * e0 + A.c2[r][p] * a0 + A.c3[r][p] * x1[o];
+                x1[o] = a0;
+                x0[o] = pn;
+            } else {
+                x0[o] = A.c1[r][p] * a0 + A.c0[r][p] * (T(0.5) * (e1 + e0));
+            }
+        }
+        e = e1;
+        return true;
+    }
+    return false;
+}
+
+template <typename T>
 static FieldArgs<T> make_field_args(pc_ctx* c, int in_set, int out_set) {
     FieldArgs<T> a{};
     const pc_grid_desc& g = c->g;

@@ -57,8 +57,8 @@ __global__ void __launch_bounds__(256) split_h3(FieldArgs<T> a, CpmlArgs<T> p) {
     }
 }
 
-template <typename T, bool CPML>
-__global__ void __launch_bounds__(256) split_e3(FieldArgs<T> a, CpmlArgs<T> p) {
+template <typename T, bool CPML, bool ADE>
+__global__ void __launch_bounds__(256) split_e3(FieldArgs<T> a, CpmlArgs<T> p, AdeArgs<T> ade) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int i = blockIdx.z;
@@ -76,7 +76,9 @@ __global__ void __launch_bounds__(256) split_e3(FieldArgs<T> a, CpmlArgs<T> p) {
             c1 = cpml3<T, 1>(p, SY_EX, q, c1);
             c2 = cpml3<T, 2>(p, SZ_EX, q, c2);
         }
-        Ex[o] = ecoef(a.ca[0], o) * Ex[o] + a.cb[0][o] * (c1 - c2);
+        T e = Ex[o];
+        if (!(ADE && ade_update(ade, 0, i, j, k, c1 - c2, e))) e = ecoef(a.ca[0], o) * e + a.cb[0][o] * (c1 - c2);
+        Ex[o] = e;
     }
     if (i < nx - 1 && k < nz - 1) {
         T c1 = (Hx[o + 1] - Hx[o]) * a.inv_dz;
@@ -85,7 +87,9 @@ __global__ void __launch_bounds__(256) split_e3(FieldArgs<T> a, CpmlArgs<T> p) {
             c1 = cpml3<T, 2>(p, SZ_EY, q, c1);
             c2 = cpml3<T, 0>(p, SX_EY, q, c2);
         }
-        Ey[o] = ecoef(a.ca[1], o) * Ey[o] + a.cb[1][o] * (c1 - c2);
+        T e = Ey[o];
+        if (!(ADE && ade_update(ade, 1, i, j, k, c1 - c2, e))) e = ecoef(a.ca[1], o) * e + a.cb[1][o] * (c1 - c2);
+        Ey[o] = e;
     }
     if (i < nx - 1 && j < ny - 1) {
         T c1 = (Hy[o + R] - Hy[o]) * a.inv_dx;
@@ -94,7 +98,9 @@ __global__ void __launch_bounds__(256) split_e3(FieldArgs<T> a, CpmlArgs<T> p) {
             c1 = cpml3<T, 0>(p, SX_EZ, q, c1);
             c2 = cpml3<T, 1>(p, SY_EZ, q, c2);
         }
-        Ez[o] = ecoef(a.ca[2], o) * Ez[o] + a.cb[2][o] * (c1 - c2);
+        T e = Ez[o];
+        if (!(ADE && ade_update(ade, 2, i, j, k, c1 - c2, e))) e = ecoef(a.ca[2], o) * e + a.cb[2][o] * (c1 - c2);
+        Ez[o] = e;
     }
 }
 
@@ -131,8 +137,8 @@ __global__ void __launch_bounds__(256) split_h2(FieldArgs<T> a, CpmlArgs<T> p) {
     }
 }
 
-template <typename T, bool CPML>
-__global__ void __launch_bounds__(256) split_e2(FieldArgs<T> a, CpmlArgs<T> p) {
+template <typename T, bool CPML, bool ADE>
+__global__ void __launch_bounds__(256) split_e2(FieldArgs<T> a, CpmlArgs<T> p, AdeArgs<T> ade) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     const int nx = a.nx, ny = a.ny;
@@ -149,17 +155,23 @@ __global__ void __launch_bounds__(256) split_e2(FieldArgs<T> a, CpmlArgs<T> p) {
             c1 = cpml2<T, 0>(p, SX_EZ, q, c1);
             c2 = cpml2<T, 1>(p, SY_EZ, q, c2);
         }
-        Ez[o] = ecoef(a.ca[2], o) * Ez[o] + a.cb[2][o] * (c1 - c2);
+        T e = Ez[o];
+        if (!(ADE && ade_update(ade, 2, i, j, 0, c1 - c2, e))) e = ecoef(a.ca[2], o) * e + a.cb[2][o] * (c1 - c2);
+        Ez[o] = e;
     }
     if (j < ny - 1) {
         T c = (Hz[o + 1] - Hz[o]) * a.inv_dy;
         if (CPML) c = cpml2<T, 1>(p, SY_EX, q, c);
-        Ex[o] = ecoef(a.ca[0], o) * Ex[o] + a.cb[0][o] * c;
+        T e = Ex[o];
+        if (!(ADE && ade_update(ade, 0, i, j, 0, c, e))) e = ecoef(a.ca[0], o) * e + a.cb[0][o] * c;
+        Ex[o] = e;
     }
     if (i < nx - 1) {
         T c = (Hz[o + P] - Hz[o]) * a.inv_dx;
         if (CPML) c = cpml2<T, 0>(p, SX_EY, q, c);
-        Ey[o] = ecoef(a.ca[1], o) * Ey[o] - a.cb[1][o] * c;
+        T e = Ey[o];
+        if (!(ADE && ade_update(ade, 1, i, j, 0, -c, e))) e = ecoef(a.ca[1], o) * e - a.cb[1][o] * c;
+        Ey[o] = e;
     }
 }
 
@@ -167,28 +179,39 @@ template <typename T>
 int split_step_t(pc_ctx* c, cudaStream_t s) {
     FieldArgs<T> a = make_field_args<T>(c, c->cur, c->cur);
     CpmlArgs<T> p = make_cpml_args<T>(c, c->cur, c->cur);
+    AdeArgs<T> ade = make_ade_args<T>(c);
     const pc_grid_desc& g = c->g;
-    const bool cp = p.t > 0;
+    const bool cp = p.t > 0, ad = ade.nreg > 0;
     if (g.ndim == 3) {
         dim3 blk(32, 8);
         dim3 grd((g.nz + 31) / 32, (g.ny + 7) / 8, g.nx);
-        if (cp) {
+        if (cp)
             split_h3<T, true><<<grd, blk, 0, s>>>(a, p);
-            split_e3<T, true><<<grd, blk, 0, s>>>(a, p);
-        } else {
+        else
             split_h3<T, false><<<grd, blk, 0, s>>>(a, p);
-            split_e3<T, false><<<grd, blk, 0, s>>>(a, p);
-        }
+        if (cp && ad)
+            split_e3<T, true, true><<<grd, blk, 0, s>>>(a, p, ade);
+        else if (cp)
+            split_e3<T, true, false><<<grd, blk, 0, s>>>(a, p, ade);
+        else if (ad)
+            split_e3<T, false, true><<<grd, blk, 0, s>>>(a, p, ade);
+        else
+            split_e3<T, false, false><<<grd, blk, 0, s>>>(a, p, ade);
     } else {
         dim3 blk(32, 8);
         dim3 grd((g.ny + 31) / 32, (g.nx + 7) / 8);
-        if (cp) {
+        if (cp)
             split_h2<T, true><<<grd, blk, 0, s>>>(a, p);
-            split_e2<T, true><<<grd, blk, 0, s>>>(a, p);
-        } else {
+        else
             split_h2<T, false><<<grd, blk, 0, s>>>(a, p);
-            split_e2<T, false><<<grd, blk, 0, s>>>(a, p);
-        }
+        if (cp && ad)
+            split_e2<T, true, true><<<grd, blk, 0, s>>>(a, p, ade);
+        else if (cp)
+            split_e2<T, true, false><<<grd, blk, 0, s>>>(a, p, ade);
+        else if (ad)
+            split_e2<T, false, true><<<grd, blk, 0, s>>>(a, p, ade);
+        else
+            split_e2<T, false, false><<<grd, blk, 0, s>>>(a, p, ade);
     }
     c->launches += 2;
     PC_CUDA_CHECK(cudaGetLastError());

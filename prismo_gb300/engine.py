@@ -46,6 +46,11 @@ def component_shape(comp: str, dims, is_2d: bool):
             "Hx": (nx - 1, ny, nz), "Hy": (nx, ny - 1, nz), "Hz": (nx, ny, nz - 1)}[comp]
 
 
+def torch_complex(re, im):
+    torch = _torch()
+    return torch.complex(re, im)
+
+
 def _round_up(x: int, m: int) -> int:
     return (x + m - 1) // m * m
 
@@ -111,6 +116,7 @@ class FDTDEngine:
         if pml is not None and int(pml.thickness) > 0:
             self._set_cpml(pml)
         self.sources = []  # (comp, offsets, weights, waveform)
+        self.dfts = []  # (comp, offsets, omegas, accumulator tensor)
         self._closed = False
 
     # -- setup ---------------------------------------------------------------
@@ -219,6 +225,59 @@ class FDTDEngine:
             None if w is None else w.ctypes.data_as(C.POINTER(C.c_double)), int(offs.size)), "pc_add_source")
         self.sources.append((comp, offs, w, waveform))
         return sid
+
+    # -- dispersive regions ----------------------------------------------------------
+    def set_dispersive(self, regions):
+        """Dispersive (ADE) regions: a list of (box, eps_inf, poles) with box =
+        (x0, x1, y0, y1, z0, z1) in each E component's own index space and poles
+        dicts from ``prismo_gb300.materials`` (kind lorentz/drude/debye with C0..C3).
+        Allocates the zeroed auxiliary arrays on the device."""
+        torch = _torch()
+        kinds = {"lorentz": 0, "drude": 1, "debye": 2}
+        arr = (_lib.AdeRegion * max(1, len(regions)))()
+        self.ade_aux = []
+        for r, (box, eps_inf, poles) in enumerate(regions):
+            R = arr[r]
+            box = [int(b) for b in box]
+            if self.is_2d:
+                box = box[:4] + [0, 1]
+            for q in range(6):
+                R.box[q] = box[q]
+            R.npoles = len(poles)
+            R.eps_inf = float(eps_inf)
+            shape = (box[1] - box[0], box[3] - box[2], box[5] - box[4])
+            for pi, p in enumerate(poles):
+                R.kind[pi] = kinds[p["kind"]]
+                R.c0[pi], R.c1[pi] = float(p["C0"]), float(p["C1"])
+                R.c2[pi], R.c3[pi] = float(p.get("C2", 0.0)), float(p.get("C3", 0.0))
+                for c in range(3):
+                    for w in range(2 if p["kind"] == "lorentz" else 1):
+                        t = torch.zeros(shape, dtype=self.dtype, device=self.device)
+                        self.ade_aux.append(t)
+                        R.aux[c][pi][w] = t.data_ptr()
+        _lib.check(self.lib.pc_set_ade(self.ctx, len(regions), arr, EPS0), "pc_set_ade")
+        self.ade_regions = regions
+
+    # -- DFT monitors ------------------------------------------------------------
+    def add_dft(self, comp: str, offsets: np.ndarray, freqs, t0: float) -> int:
+        """Device DFT running sum of ``comp`` at ``offsets`` for ``freqs`` (Hz); the
+        first sample is taken after the next step, at simulation time ``t0``."""
+        torch = _torch()
+        offs = np.ascontiguousarray(offsets, dtype=np.int64)
+        om = np.ascontiguousarray(2 * np.pi * np.asarray(freqs, dtype=np.float64))
+        acc = torch.zeros((len(om), offs.size, 4), dtype=torch.float32, device=self.device)
+        mid = _lib.check(self.lib.pc_add_dft(
+            self.ctx, COMP_INDEX[comp], offs.ctypes.data_as(C.POINTER(C.c_int64)), int(offs.size),
+            om.ctypes.data_as(C.POINTER(C.c_double)), int(om.size), self.dt, float(t0), acc.data_ptr()),
+            "pc_add_dft")
+        self.dfts.append((comp, offs, om, acc))
+        return mid
+
+    def dft_result(self, mid: int):
+        """Complex (nf, npts) accumulator of a DFT monitor (flushes pending samples)."""
+        _lib.check(self.lib.pc_dft_flush(self.ctx, int(mid), self._stream_ptr()), "pc_dft_flush")
+        acc = self.dfts[mid][3].double()
+        return torch_complex(acc[..., 0] - acc[..., 2], acc[..., 1] - acc[..., 3])
 
     # -- stepping --------------------------------------------------------------
     def step(self, nsteps: int = 1, amps: Optional[np.ndarray] = None):
