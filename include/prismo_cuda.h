@@ -144,6 +144,16 @@ typedef struct pc_ade_region {
 
 int pc_set_ade(pc_ctx* ctx, int32_t nregions, const pc_ade_region* regions, double eps0);
 
+/* Plane-wave TFSF source on the plane k = k0 (3D, corrected stepper), fed by a
+ * 1D auxiliary Yee line of aux_len points with the same dz and dt in a medium of
+ * relative permittivity eps_b, sampled at index m0 (replaces the single-plane
+ * correction of sources/tfsf.py:258-411).  direction = +1/-1 (propagation along
+ * +z/-z), polarization 0 = Ex/Hy, 1 = Ey/Hx.  Its waveform amplitude a(t_{n+1})
+ * is the last column of the pc_step amplitude table.  The plane must lie outside
+ * the z CPML and dispersive regions. */
+int pc_set_tfsf(pc_ctx* ctx, int32_t k0, int32_t direction, int32_t polarization, int32_t m0, int32_t aux_len,
+                double eps_b, double eps0);
+
 /* DFT monitor (monitors/field.py:138-143, monitors/dft.py:108-137): after every
  * step (and after the sources) F_f += field(t_{n+1}) exp(-i omega_f t_{n+1}) dt at
  * the npts element offsets of component comp.  t0 is t_{n+1} of the next step.

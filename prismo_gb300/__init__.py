@@ -20,5 +20,18 @@ from .sources import (  # noqa: F401,E402
     PlaneWaveSource,
     PointSource,
     Source,
+    TFSFSource,
     Waveform,
 )
+from .backend import CudaBackend, DeviceArray, get_backend, get_backend_info, list_available_backends, set_backend  # noqa
+from .fields import ElectromagneticFields  # noqa: F401,E402
+from .materials import (  # noqa: F401,E402
+    DebyeMaterial,
+    DrudeLorentzMaterial,
+    DrudeMaterial,
+    LorentzMaterial,
+    LorentzPole,
+)
+from .monitors import DFTMonitor, FieldMonitor, Monitor  # noqa: F401,E402
+from .simulation import Simulation  # noqa: F401,E402
+from .solver import FDTDSolver, MaxwellUpdater  # noqa: F401,E402

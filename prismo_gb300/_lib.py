@@ -86,6 +86,8 @@ SIGNATURES = {
     "pc_set_cpml": (C.c_int, [C.c_void_p, C.c_int32, DPP, DPP, DPP, C.c_void_p, C.c_void_p]),
     "pc_add_source": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.c_int32]),
     "pc_step": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_void_p]),
+    "pc_set_tfsf": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double,
+                              C.c_double]),
     "pc_set_ade": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(AdeRegion), C.c_double]),
     "pc_add_dft": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_double),
                              C.c_int32, C.c_double, C.c_double, C.c_void_p]),

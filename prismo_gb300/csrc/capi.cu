@@ -102,6 +102,8 @@ void pc_destroy(pc_ctx* c) {
     cudaFree(c->d_amps);
     cudaFree(c->d_cpml_coef);
     cudaFree(c->d_cpml_slab);
+    cudaFree(c->tfsf.d_e1);
+    cudaFree(c->tfsf.d_h1);
     cudaFree(c->d_status);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
     destroy_fused_state(c);
@@ -260,9 +262,17 @@ int pc_step(pc_ctx* c, int32_t nsteps, const double* amps, void* stream) {
     if (!c->have_fields || !c->have_coef) return PC_ERR_STATE;
     cudaStream_t s = (cudaStream_t)stream;
     const size_t ns = c->sources.size();
+    const size_t ncol = ns + (c->tfsf.on ? 1 : 0);  // the TFSF amplitude is the last column
+    if (c->tfsf.on && !amps) return PC_ERR_INVALID;
     if (ns > 0) {
         if (!amps) return PC_ERR_INVALID;
         const size_t need = (size_t)nsteps * ns;
+        if (ncol != ns) {  // repack the source columns (the kernel reads a [nsteps][ns] table)
+            c->amps_host.resize(need);
+            for (int n = 0; n < nsteps; ++n)
+                for (size_t q = 0; q < ns; ++q) c->amps_host[(size_t)n * ns + q] = amps[(size_t)n * ncol + q];
+        }
+        const double* src_tab = ncol != ns ? c->amps_host.data() : amps;
         if (need > c->amps_cap) {
             PC_CUDA_CHECK(cudaStreamSynchronize(s));
             cudaFree(c->d_amps);
@@ -271,7 +281,8 @@ int pc_step(pc_ctx* c, int32_t nsteps, const double* amps, void* stream) {
             PC_CUDA_CHECK(cudaMalloc(&c->d_amps, need * sizeof(double)));
             c->amps_cap = need;
         }
-        if (need) PC_CUDA_CHECK(cudaMemcpyAsync(c->d_amps, amps, need * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (need) PC_CUDA_CHECK(cudaMemcpyAsync(c->d_amps, src_tab, need * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (ncol != ns) PC_CUDA_CHECK(cudaStreamSynchronize(s));  // amps_host is reused by the next call
     }
     for (int n = 0; n < nsteps; ++n) {
         int rc;
@@ -289,12 +300,13 @@ int pc_step(pc_ctx* c, int32_t nsteps, const double* amps, void* stream) {
             c->prof_used += 2;
             PC_CUDA_CHECK(cudaEventRecord(ev0, s));
         }
+        const double* tamp = c->tfsf.on ? &amps[(size_t)n * ncol + ns] : nullptr;
         if (c->g.mode == PC_MODE_LEGACY)
             rc = launch_legacy_step(c, s);
-        else if (c->g.sched == PC_SCHED_FUSED && c->ade_n == 0)
+        else if (c->g.sched == PC_SCHED_FUSED && c->ade_n == 0 && !c->tfsf.on)
             rc = launch_fused_step(c, s);
         else
-            rc = launch_split_step(c, s);
+            rc = launch_split_step(c, s, tamp);
         if (rc) return rc;
         if (ev1) PC_CUDA_CHECK(cudaEventRecord(ev1, s));
         rc = launch_sources(c, n, s);
@@ -384,6 +396,31 @@ int pc_set_ade(pc_ctx* c, int32_t n, const pc_ade_region* regs, double eps0) {
     }
     c->ade_n = n;
     c->ade_sdt = dt / eps0;
+    return PC_OK;
+}
+
+int pc_set_tfsf(pc_ctx* c, int32_t k0, int32_t direction, int32_t polarization, int32_t m0, int32_t aux_len,
+                double eps_b, double eps0) {
+    if (!c || c->g.ndim != 3 || c->g.mode != PC_MODE_CORRECTED) return PC_ERR_INVALID;
+    if (direction != 1 && direction != -1) return PC_ERR_INVALID;
+    if (polarization != 0 && polarization != 1) return PC_ERR_INVALID;
+    if (k0 < 1 || k0 > c->g.nz - 3 || m0 < 1 || aux_len < m0 + 3 || !(eps_b > 0) || !(eps0 > 0))
+        return PC_ERR_INVALID;
+    const size_t es = (size_t)c->g.precision;
+    cudaFree(c->tfsf.d_e1);
+    cudaFree(c->tfsf.d_h1);
+    c->tfsf = TfsfState{};
+    PC_CUDA_CHECK(cudaMalloc(&c->tfsf.d_e1, aux_len * es));
+    PC_CUDA_CHECK(cudaMalloc(&c->tfsf.d_h1, aux_len * es));
+    PC_CUDA_CHECK(cudaMemset(c->tfsf.d_e1, 0, aux_len * es));
+    PC_CUDA_CHECK(cudaMemset(c->tfsf.d_h1, 0, aux_len * es));
+    c->tfsf.on = true;
+    c->tfsf.k0 = k0;
+    c->tfsf.dir = direction;
+    c->tfsf.pol = polarization;
+    c->tfsf.m0 = m0;
+    c->tfsf.M = aux_len;
+    c->tfsf.cb1 = c->g.dt / (eps0 * eps_b);
     return PC_OK;
 }
 

@@ -58,6 +58,15 @@ struct AdeArgs {
     T* aux[PC_MAX_ADE_REGIONS][3][PC_MAX_ADE_POLES][2];
 };
 
+// TFSF plane source state (see tfsf.cu).
+struct TfsfState {
+    bool on;
+    int k0, dir, pol, m0, M;
+    double cb1;
+    void* d_e1;  // auxiliary E line [M] (ctx-owned)
+    void* d_h1;  // auxiliary H line [M] (ctx-owned)
+};
+
 // Geometry of the slab-only psi storage.  Axis a keeps four slots; the lower
 // slab index s = idx (idx < t), the upper s = idx - (n - 2t) (idx >= n - t).
 struct PsiLayout {
@@ -119,6 +128,8 @@ struct pc_ctx {
     void* psi[2];
     void* d_cpml_coef;  // [3 axes][b, a, kinv][n_axis] in context precision
     void* d_cpml_slab;  // [3 axes][b, a, kinv][2t]: the same values at slab indices only
+    // TFSF plane source; its amplitude is the last column of the pc_step table
+    pc::TfsfState tfsf;
     // dispersive regions (host copy, converted per launch)
     int ade_n;
     pc_ade_region ade[PC_MAX_ADE_REGIONS];
@@ -128,6 +139,7 @@ struct pc_ctx {
     std::vector<pc::DftMonitor> dfts;
     double* d_amps;
     size_t amps_cap;
+    std::vector<double> amps_host;  // repacked source columns when a TFSF column is present
     // fused schedule: cached tensor maps and the chosen x-chunk length
     void* fused_state;
     int fused_cx;
@@ -150,7 +162,9 @@ int launch_build_coefficients(const pc_grid_desc& g, const double* eps, const do
                               void* const db[3], cudaStream_t s, int64_t* launches);
 
 int launch_legacy_step(pc_ctx* c, cudaStream_t s);
-int launch_split_step(pc_ctx* c, cudaStream_t s);
+int launch_split_step(pc_ctx* c, cudaStream_t s, const double* tfsf_amp = nullptr);
+int launch_tfsf_h(pc_ctx* c, cudaStream_t s);
+int launch_tfsf_e(pc_ctx* c, double amp, cudaStream_t s);
 int launch_sources(pc_ctx* c, int step_in_batch, cudaStream_t s);
 int launch_fused_step(pc_ctx* c, cudaStream_t s);
 void destroy_fused_state(pc_ctx* c);

@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(256) split_e2(FieldArgs<T> a, CpmlArgs<T> p, A
 }
 
 template <typename T>
-int split_step_t(pc_ctx* c, cudaStream_t s) {
+int split_step_t(pc_ctx* c, cudaStream_t s, const double* tfsf_amp) {
     FieldArgs<T> a = make_field_args<T>(c, c->cur, c->cur);
     CpmlArgs<T> p = make_cpml_args<T>(c, c->cur, c->cur);
     AdeArgs<T> ade = make_ade_args<T>(c);
@@ -189,6 +189,10 @@ int split_step_t(pc_ctx* c, cudaStream_t s) {
             split_h3<T, true><<<grd, blk, 0, s>>>(a, p);
         else
             split_h3<T, false><<<grd, blk, 0, s>>>(a, p);
+        if (tfsf_amp) {
+            const int rc = launch_tfsf_h(c, s);
+            if (rc) return rc;
+        }
         if (cp && ad)
             split_e3<T, true, true><<<grd, blk, 0, s>>>(a, p, ade);
         else if (cp)
@@ -197,6 +201,10 @@ int split_step_t(pc_ctx* c, cudaStream_t s) {
             split_e3<T, false, true><<<grd, blk, 0, s>>>(a, p, ade);
         else
             split_e3<T, false, false><<<grd, blk, 0, s>>>(a, p, ade);
+        if (tfsf_amp) {
+            const int rc = launch_tfsf_e(c, *tfsf_amp, s);
+            if (rc) return rc;
+        }
     } else {
         dim3 blk(32, 8);
         dim3 grd((g.ny + 31) / 32, (g.nx + 7) / 8);
@@ -220,8 +228,8 @@ int split_step_t(pc_ctx* c, cudaStream_t s) {
 
 }  // namespace
 
-int launch_split_step(pc_ctx* c, cudaStream_t s) {
-    return c->g.precision == 8 ? split_step_t<double>(c, s) : split_step_t<float>(c, s);
+int launch_split_step(pc_ctx* c, cudaStream_t s, const double* tfsf_amp) {
+    return c->g.precision == 8 ? split_step_t<double>(c, s, tfsf_amp) : split_step_t<float>(c, s, tfsf_amp);
 }
 
 }  // namespace pc

@@ -46,6 +46,19 @@ def component_shape(comp: str, dims, is_2d: bool):
             "Hx": (nx - 1, ny, nz), "Hy": (nx, ny - 1, nz), "Hz": (nx, ny, nz - 1)}[comp]
 
 
+def new_field_sets(buf_shape, dtype, device, n):
+    torch = _torch()
+    return [torch.zeros(buf_shape, dtype=dtype, device=device) for _ in range(n)]
+
+
+def storage_shape(dims, is_2d: bool):
+    """Padded field-set shape: (6, nx, pitch) in 2D, (6, nx, ny, pitch) in 3D."""
+    nx, ny, nz = dims
+    if is_2d:
+        return (6, nx, _round_up(ny, 32))
+    return (6, nx, ny, _round_up(nz, 32))
+
+
 def torch_complex(re, im):
     torch = _torch()
     return torch.complex(re, im)
@@ -61,7 +74,7 @@ class FDTDEngine:
     def __init__(self, dims: Sequence[int], spacing: Sequence[float], dt: float, *, is_2d: bool,
                  precision: str = "fp32", mode: str = "corrected", sched: str = "auto",
                  material_arrays: Optional[dict] = None, pml: Optional[PMLParams] = None,
-                 device: str = "cuda:0", stream=None):
+                 device: str = "cuda:0", stream=None, sets=None, bind_later: bool = False):
         torch = _torch()
         self.lib = _lib.load()
         if not torch.cuda.is_available():
@@ -103,13 +116,11 @@ class FDTDEngine:
         # the library resolves AUTO; ping-pong sets are needed for the fused 3D schedule
         self.pingpong = (not self.is_2d) and self.mode == _lib.PC_MODE_CORRECTED and \
             self.sched in (_lib.PC_SCHED_AUTO, _lib.PC_SCHED_FUSED)
-        with torch.cuda.device(self.device):
-            self.sets = [torch.zeros(self.buf_shape, dtype=self.dtype, device=self.device)]
-            if self.pingpong:
-                self.sets.append(torch.zeros(self.buf_shape, dtype=self.dtype, device=self.device))
-        s0 = _lib.P6(*[self.sets[0][q].data_ptr() for q in range(6)])
-        s1 = _lib.P6(*[self.sets[1][q].data_ptr() for q in range(6)]) if self.pingpong else None
-        _lib.check(self.lib.pc_set_fields(self.ctx, s0, s1), "pc_set_fields")
+        self.sets = []
+        if not bind_later:
+            if sets is None:
+                sets = new_field_sets(self.buf_shape, self.dtype, self.device, 2 if self.pingpong else 1)
+            self.bind(sets, 0)
         self._set_materials(material_arrays)
         self.pml = None
         self.psi = []
@@ -120,6 +131,24 @@ class FDTDEngine:
         self._closed = False
 
     # -- setup ---------------------------------------------------------------
+    def bind(self, sets, cur: int = 0):
+        """Attach field storage: a list of one or two tensors of shape buf_shape
+        (a second set is allocated when the schedule ping-pongs)."""
+        sets = list(sets)
+        for t in sets:
+            if tuple(t.shape) != tuple(self.buf_shape) or t.dtype != self.dtype or not t.is_contiguous():
+                raise ValueError(f"field storage must be contiguous {self.dtype} of shape {self.buf_shape}")
+        if self.pingpong and len(sets) < 2:
+            sets.append(new_field_sets(self.buf_shape, self.dtype, self.device, 1)[0])
+            if cur == 1:
+                raise ValueError("current set 1 without a second set")
+        self.sets = sets
+        s0 = _lib.P6(*[sets[0][q].data_ptr() for q in range(6)])
+        s1 = _lib.P6(*[sets[1][q].data_ptr() for q in range(6)]) if self.pingpong else None
+        _lib.check(self.lib.pc_set_fields(self.ctx, s0, s1), "pc_set_fields")
+        if cur:
+            _lib.check(self.lib.pc_set_current_set(self.ctx, int(cur)), "pc_set_current_set")
+
     def _set_materials(self, ma: Optional[dict]):
         torch = _torch()
         ma = ma or {}
@@ -258,6 +287,20 @@ class FDTDEngine:
         _lib.check(self.lib.pc_set_ade(self.ctx, len(regions), arr, EPS0), "pc_set_ade")
         self.ade_regions = regions
 
+    # -- TFSF plane ------------------------------------------------------------------
+    def set_tfsf(self, k0: int, direction: int, polarization: str, waveform, eps_b: float = 1.0, m0: int = 4,
+                 max_steps: int = 20000):
+        """Plane-wave TFSF injection at z-plane k0 (see pc_set_tfsf); the auxiliary
+        line is long enough that its far-end reflection cannot reach the sample
+        point within ``max_steps`` steps."""
+        import math
+
+        C0_ = 299792458.0
+        m = m0 + int(math.ceil(0.5 * max_steps * C0_ * self.dt / self.spacing[2])) + 8
+        _lib.check(self.lib.pc_set_tfsf(self.ctx, int(k0), int(direction), 0 if polarization == "x" else 1,
+                                        int(m0), int(m), float(eps_b), EPS0), "pc_set_tfsf")
+        self.tfsf = waveform
+
     # -- DFT monitors ------------------------------------------------------------
     def add_dft(self, comp: str, offsets: np.ndarray, freqs, t0: float) -> int:
         """Device DFT running sum of ``comp`` at ``offsets`` for ``freqs`` (Hz); the
@@ -283,7 +326,7 @@ class FDTDEngine:
     def step(self, nsteps: int = 1, amps: Optional[np.ndarray] = None):
         """Advance nsteps; amps[nsteps, nsources] are the source amplitudes at
         t_{n+1} of each step (sources/point.py:62-73)."""
-        ns = len(self.sources)
+        ns = len(self.sources) + (1 if getattr(self, "tfsf", None) is not None else 0)
         ap = None
         if ns:
             a = np.ascontiguousarray(amps, dtype=np.float64).reshape(nsteps, ns)

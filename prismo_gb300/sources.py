@@ -232,6 +232,44 @@ class LineSource(Source):
         return [(self.component, idx, w, _identity)]
 
 
+class TFSFSource(Source):
+    """Plane-wave total-field/scattered-field source (sources/tfsf.py:17-411
+    interface).  On the device it is a consistent TFSF plane fed by a 1D auxiliary
+    Yee line (pc_set_tfsf); the plane is the z-index of ``center`` and propagation
+    is along +z or -z (the reference's entry-plane correction is replaced)."""
+
+    def __init__(self, center, size, direction: str, polarization: str, frequency: float, pulse: bool = True,
+                 pulse_width: Optional[float] = None, amplitude: float = 1.0, phase: float = 0.0,
+                 eps_background: float = 1.0, name: Optional[str] = None, enabled: bool = True):
+        super().__init__(center=center, size=size, name=name, enabled=enabled)
+        sign = -1 if direction.startswith("-") else 1
+        axis = direction.lstrip("+-").lower()
+        if axis != "z":
+            raise NotImplementedError("the device TFSF plane propagates along z")
+        if polarization.lower() not in ("x", "y"):
+            raise ValueError("polarization must be x or y for z propagation")
+        self.direction, self.direction_sign = axis, sign
+        self.polarization = polarization.lower()
+        self.frequency = frequency
+        self.wavelength = 299792458.0 / frequency
+        self.eps_background = eps_background
+        if pulse:
+            if pulse_width is None:
+                raise ValueError("pulse_width must be provided for pulsed sources")
+            self.waveform = GaussianPulse(frequency, pulse_width, amplitude, phase)
+        else:
+            self.waveform = ContinuousWave(frequency, amplitude, phase)
+
+    def plane_index(self) -> int:
+        return self._grid.point_to_index(self.center)[2]
+
+    def injections(self):
+        return []
+
+    def update_fields(self, fields, time, dt):
+        raise NotImplementedError("the TFSF plane runs inside the device stepper")
+
+
 def amplitude_table(sources: Sequence[Source], times: np.ndarray) -> np.ndarray:
     """[len(times), n_injections] amplitudes (disabled sources contribute 0)."""
     cols = []

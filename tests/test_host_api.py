@@ -1,0 +1,89 @@
+"""Host-side logic of the package on CPU (no GPU): grid semantics, CPML profiles,
+source amplitude tables, backend registry."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import fdtd64 as O
+
+
+def test_grid_mirror_matches_reference_fixture(golden_dir):
+    from prismo_gb300.grid import GridSpec, YeeGrid
+
+    z = np.load(os.path.join(golden_dir, "ref_scalars.npz"))
+    for r in json.loads(str(z["grids"])):
+        g = YeeGrid(GridSpec(size=tuple(r["size"]), resolution=r["res"], boundary_layers=r["layers"]))
+        assert list(g.dimensions) == r["dims"]
+        for c, s in r["shapes"].items():
+            assert list(g.get_field_shape(c)) == s
+        assert g.suggest_time_step(0.5) == r["dt05"]
+        size = r["size"]
+        pts = [(0.0, 0.0, 0.0), (size[0] / 2, size[1] / 2, size[2] / 2), (size[0], size[1], size[2]),
+               (-1e-6, 3e-6, 0.1e-6)]
+        assert [list(g.point_to_index(p)) for p in pts] == r["p2i"]
+        for c, want in r["idx"].items():
+            got = [list(map(int, np.ravel(i))) for i in g.get_component_indices(c, 3, 9, 2, 5, 1, 4)]
+            assert got == want
+
+
+def test_cpml_coefficients_match_oracle():
+    from prismo_gb300.pml import PMLParams, cpml_axis_coefficients
+
+    for n, t in [(64, 8), (256, 12), (30, 3)]:
+        b, a, k = cpml_axis_coefficients(n, PMLParams(thickness=t), 20e-9, 1.9e-17)
+        b2, a2, k2 = O.cpml_profile(n, t, 20e-9, 1.9e-17)
+        np.testing.assert_allclose(b, b2, rtol=1e-15)
+        np.testing.assert_allclose(a, a2, rtol=1e-15, atol=0)
+        np.testing.assert_allclose(k, k2, rtol=1e-15)
+
+
+def test_source_amplitudes_follow_reference_expressions():
+    from prismo_gb300.grid import YeeGrid
+    from prismo_gb300.sources import ElectricDipole, PlaneWaveSource, amplitude_table
+
+    g = YeeGrid.from_total((40, 30, 1), 20e-9, 5)
+    d = ElectricDipole(position=(0.2e-6, 0.2e-6, 0.0), polarization="z", frequency=193e12, pulse_width=5e-15)
+    pw = PlaneWaveSource(center=(0.2e-6, 0.2e-6, 0), size=(0, 0.3e-6, 0), direction="-x", polarization="z",
+                         frequency=193e12, pulse_width=5e-15)
+    for s in (d, pw):
+        s.initialize(g)
+    t = np.cumsum(np.full(50, 3e-17))
+    tab = amplitude_table([d, pw], t)
+    wf = O.gaussian_pulse(193e12, 5e-15)
+    np.testing.assert_array_equal(tab[:, 0], [wf(x) for x in t])
+    np.testing.assert_array_equal(tab[:, 1], [wf(x) * -1 for x in t])
+    np.testing.assert_array_equal(tab[:, 2], [(wf(x) / 377.0) * -1 for x in t])
+
+
+def test_backend_registry_without_gpu():
+    import torch
+
+    from prismo_gb300 import backend
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    assert backend.list_available_backends() == []
+    with pytest.raises(ValueError):
+        backend.set_backend("cuda")
+    with pytest.raises(ValueError):
+        backend.set_backend("numpy")
+
+
+def test_materials_match_reference_coefficients(golden_dir):
+    from prismo_gb300.materials import DebyeMaterial, DrudeMaterial, LorentzMaterial, LorentzPole
+
+    z = np.load(os.path.join(golden_dir, "ref_scalars.npz"))
+    dt = float(z["ade_dt"])
+    lor = LorentzMaterial(1.5, [LorentzPole(omega_0=w0, gamma=g, delta_epsilon=de) for w0, g, de in z["lorentz_params"]])
+    got = np.array([[p[k] for k in ("C0", "C1", "C2", "C3")] for p in lor.get_ade_coefficients(dt)["poles"]])
+    np.testing.assert_allclose(got, z["lorentz"], rtol=1e-15)
+    c = DrudeMaterial(1.0, 1.37e16, 1.0e14).get_ade_coefficients(dt)
+    np.testing.assert_allclose([c["C0"], c["C1"]], z["drude"], rtol=1e-15)
+    c = DebyeMaterial(2.0, 5.0, 3e-15).get_ade_coefficients(dt)
+    np.testing.assert_allclose([c["C0"], c["C1"]], z["debye"], rtol=1e-15)
+    np.testing.assert_allclose(lor.permittivity(z["eps_w"]), z["eps_lorentz"], rtol=1e-13)
+    np.testing.assert_allclose(DrudeMaterial(1.0, 1.37e16, 1.0e14).permittivity(z["eps_w"]), z["eps_drude"],
+                               rtol=1e-13)

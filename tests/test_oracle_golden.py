@@ -122,3 +122,22 @@ def test_grid_semantics_match_reference(golden_dir):
         for c, want in r["idx"].items():
             got = [list(map(int, np.ravel(i))) for i in g.component_indices(c, 3, 9, 2, 5, 1, 4)]
             assert got == want
+
+
+def test_oracle_tfsf_keeps_scattered_region_dark():
+    """In vacuum with nothing to scatter, the scattered-field side of the TFSF plane
+    stays dark at the centre of the cross-section while the total-field side carries
+    the incident pulse; what reaches the scattered side is diffraction from the
+    plane's transverse edges (the plane spans the whole cross-section)."""
+    g = O.OracleGrid.from_total(48, 48, 72, 20e-9, 8)
+    dt = g.suggest_dt(0.5)
+    wf = O.gaussian_pulse(193e12, 1e-15)
+    o = O.OracleFDTD(g, dt, cpml_layers=8, tfsf=O.TFSFPlane(k0=54, direction=-1, polarization="x", waveform=wf))
+    tf = sf = 0.0
+    for _ in range(230):
+        o.step()
+        col = o.F["Ex"][24, 23, :]
+        tf = max(tf, np.abs(col[30:52]).max())
+        sf = max(sf, np.abs(col[56:63]).max())
+    assert tf > 0.3
+    assert sf < 1e-2 * tf
