@@ -77,3 +77,69 @@ def config_3d_inputs(dims=None, seed=0):
         cfg["dims"] = tuple(dims)
     eps = boxes_3d(cfg["dims"], nboxes=cfg["nboxes"], seed=seed)
     return cfg, eps
+
+
+# -- the 2D TE drop-in configuration: 500x250 total, 20-cell CPML, 3000 steps --------
+CONFIG_2D = {
+    "name": "2d_te_waveguide_500x250",
+    "dims": (500, 250, 1),
+    "dx": 20e-9,
+    "cpml": 20,
+    "steps": 3000,
+    "courant": 0.5,
+    "pulse_f0": 193e12,
+    "pulse_width": 10e-15,
+    "nfreq": 11,
+}
+
+
+def config_2d_layout(dims=(500, 250, 1), cpml=20, dx=20e-9):
+    """Slab waveguide along x (Si 0.5 um in SiO2); soft Ez line source across the
+    slab at x = cpml + 10, DFT line (all y) at x = nx - cpml - 10, 11 frequencies
+    for wavelengths 1.5-1.6 um.  Index sets are in Ez's own indices."""
+    nx, ny = dims[0], dims[1]
+    eps = slab_waveguide_2d(dims, dx)
+    core = np.nonzero(_axis_mask(ny, ny / 2.0, 0.5e-6 / dx))[0]
+    src = (np.array([cpml + 10]).reshape(1, 1), core.reshape(1, -1))
+    mon = (np.array([nx - cpml - 10]).reshape(1, 1), np.arange(ny - 1).reshape(1, -1))
+    freqs = wavelengths_to_freqs(1.5e-6, 1.6e-6, 11)
+    return eps, src, mon, freqs
+
+
+# -- the 3D dispersive configuration: 384x384x192, Drude-Lorentz metal, TFSF ----------
+CONFIG_3D_DISPERSIVE = {
+    "name": "3d_dispersive_384x384x192",
+    "dims": (384, 384, 192),
+    "dx": 20e-9,
+    "cpml": 12,
+    "steps": 4000,
+    "z_metal": 96,
+    "ridge_width": 1.0e-6,
+    "ridge_height": 0.4e-6,
+    "eps_ridge": 4.0,
+    "omega_p": 1.37e16,
+    "gamma_d": 1.0e14,
+    "nfreq": 64,
+}
+
+
+def config_3d_dispersive(dims=(384, 384, 192), seed=0, dx=20e-9, z_metal=None):
+    """Half-space Drude + 2-Lorentz metal (z < z_metal, eps_inf = 1), a Si3N4 ridge
+    (eps 4.0, 1 um wide along y, 0.4 um high) on it, air above; seeded Lorentz
+    poles (omega0 U[3e15, 6e15], delta_eps U[0.5, 2], gamma U[1e14, 5e14]).
+    Returns eps (cell-centred), the metal box (E indices), the pole list
+    (materials.LorentzPole) and the TFSF plane index (above the ridge, -z)."""
+    from .materials import LorentzPole
+
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = dims
+    zm = z_metal if z_metal is not None else nz // 2
+    eps = np.ones(dims)
+    ridge_h = int(round(0.4e-6 / dx))
+    my = _axis_mask(ny, ny / 2.0, 1.0e-6 / dx)
+    eps[:, my, zm:zm + ridge_h] = 4.0
+    lor = [LorentzPole(omega_0=rng.uniform(3e15, 6e15), delta_epsilon=rng.uniform(0.5, 2.0),
+                       gamma=rng.uniform(1e14, 5e14)) for _ in range(2)]
+    box = (0, nx, 0, ny, 0, zm)
+    k_plane = min(nz - 12 - 8, zm + ridge_h + (nz - zm - ridge_h) // 2)
+    return eps, box, lor, k_plane
