@@ -208,6 +208,82 @@ int pc_profile_read(pc_ctx* ctx, double* total_ms, int64_t* count);
 int pc_fused_steps_noalloc(const pc_grid_desc* desc, void* const set0[6], void* const set1[6], int32_t cur,
                            const void* const cb[3], int32_t nsteps, void* stream, uint32_t* status_out);
 
+/* ------------------------------------------------------------------------- *
+ * Batched 2D sweep.  Replaces the per-design loop of ParameterSweep
+ * (optimization/sweep.py:41-195, one Simulation.run per design, sequential or
+ * in a process pool) for 2D TE designs (Ez, Hx, Hy; core/solver.py:311-456,
+ * corrected stencil) that share dx, dy, dt and the CPML thickness but not their
+ * grid size.  All instances advance together: one persistent kernel per pass
+ * covers every (instance, tile) item and runs K steps per pass; the time loop
+ * is replayed from a captured CUDA graph of G steps.  Float32 fields, lossless
+ * non-magnetic media (Ca = 1, Da = 1, Db = db_s).
+ *
+ * Per-instance device layout (offsets from pc_batch_instance_offsets):
+ *   field set: Ez, Hx, Hy, each [nx][pitch] (pitch = ny rounded up to 32),
+ *              at field_offset + q * nx * pitch (q = 0, 1, 2)
+ *   Cb(Ez):    [nx][pitch] at coef_offset
+ * Each instance has one soft Ez line source (Ez index src_x, y in
+ * [src_y0, src_y0 + src_n)) with per-point weights, all driven by one amplitude
+ * table a(t_{n+1}) (sources/point.py:62-73), and up to four DFT port lines of Ez
+ * (x = port_x, y in [port_y0, port_y0 + port_n)) at shared frequencies.
+ * ------------------------------------------------------------------------- */
+typedef struct pc_batch pc_batch;
+
+typedef struct pc_batch_instance {
+    int32_t nx, ny;               /* total Yee dimensions (2D) */
+    int32_t src_x, src_y0, src_n; /* soft Ez line source */
+    int32_t nport;                /* 0..4 */
+    int32_t port_x[4], port_y0[4], port_n[4];
+} pc_batch_instance;
+
+typedef struct pc_batch_layout {
+    int64_t field_elems;  /* floats in one field set (all instances) */
+    int64_t coef_elems;   /* floats in the Cb(Ez) buffer */
+    int64_t psi_elems;    /* floats in one CPML auxiliary buffer */
+    int64_t weight_elems; /* source weights of all instances (doubles) */
+    int64_t dft_points;   /* port points of all instances */
+} pc_batch_layout;
+
+/* Describe the batch (host only, plus small descriptor buffers).  db_s =
+ * dt / mu0.  `lay` receives the sizes of the caller-owned buffers. */
+int pc_batch_create(int32_t ninst, const pc_batch_instance* inst, int32_t cpml_t, double dx, double dy, double dt,
+                    double db_s, pc_batch** out, pc_batch_layout* lay);
+/* out = {field offset, pitch, coef offset, first weight, first DFT point} */
+int pc_batch_instance_offsets(const pc_batch* b, int32_t i, int64_t out[5]);
+/* Two zeroed field sets, the Cb buffer and (cpml_t > 0) two zeroed CPML buffers. */
+int pc_batch_bind(pc_batch* b, void* d_set0, void* d_set1, void* d_cb, void* d_psi0, void* d_psi1);
+/* Cb(Ez) of instance i from its cell-centred relative permittivity d_eps
+ * (device float64 [nx][ny]), core/solver.py:113-133 + 4-point Ez average. */
+int pc_batch_build_coefficients(pc_batch* b, int32_t i, const double* d_eps, double eps0, void* stream);
+/* CPML recursion coefficients by slab index (2 * cpml_t entries each: lower
+ * slab cells 0..t-1, then upper slab cells n-t..n-1), shared by both axes. */
+int pc_batch_set_cpml(pc_batch* b, const double* bcoef, const double* acoef, const double* kappa);
+/* Source weights (weight_elems doubles, instance-major) and the amplitude table
+ * a(t_{n+1}) of steps 0..namps-1 (0 after the table). */
+int pc_batch_set_sources(pc_batch* b, const double* weights, const double* amps, int32_t namps);
+/* Port DFT of every instance's port lines (Ez) at nf angular frequencies; t0 is
+ * t_{n+1} of the next step; d_acc is caller-owned zeroed float
+ * [nf][dft_points][4] as in pc_add_dft.  Point order: instance, port, y. */
+int pc_batch_set_dft(pc_batch* b, const double* omega, int32_t nf, double t0, void* d_acc);
+/* Kernel variants: tile (TX x TY cells) and steps per pass K. */
+int pc_batch_num_variants(void);
+int pc_batch_variant_info(int32_t variant, int32_t out[3]);
+/* graph_steps: steps per captured graph (a multiple of 16 with an even number of
+ * passes), 0 = no graph. */
+int pc_batch_set_tuning(pc_batch* b, int32_t variant, int32_t graph_steps);
+int pc_batch_get_tuning(const pc_batch* b, int32_t* variant, int32_t* graph_steps);
+/* Time `passes` dry passes (no source, no sampling; the current state is not
+ * changed) of every variant and select the fastest per step; ms_per_step
+ * (nullable) receives pc_batch_num_variants() values. */
+int pc_batch_autotune(pc_batch* b, int32_t passes, float* ms_per_step, void* stream);
+int pc_batch_step(pc_batch* b, int32_t nsteps, void* stream);
+int pc_batch_dft_flush(pc_batch* b, void* stream);
+int pc_batch_current_set(const pc_batch* b);
+int pc_batch_status(pc_batch* b, uint32_t* flags, void* stream);
+int64_t pc_batch_launch_count(const pc_batch* b);
+int64_t pc_batch_steps_done(const pc_batch* b);
+void pc_batch_destroy(pc_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

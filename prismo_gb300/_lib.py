@@ -72,6 +72,30 @@ VPP = C.POINTER(C.c_void_p)  # void* const x[n]
 DPP = C.POINTER(C.POINTER(C.c_double))  # const double* const x[3]
 
 # name -> (restype, argtypes); every symbol declared in include/prismo_cuda.h
+class BatchInstance(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32),
+        ("ny", C.c_int32),
+        ("src_x", C.c_int32),
+        ("src_y0", C.c_int32),
+        ("src_n", C.c_int32),
+        ("nport", C.c_int32),
+        ("port_x", C.c_int32 * 4),
+        ("port_y0", C.c_int32 * 4),
+        ("port_n", C.c_int32 * 4),
+    ]
+
+
+class BatchLayout(C.Structure):
+    _fields_ = [
+        ("field_elems", C.c_int64),
+        ("coef_elems", C.c_int64),
+        ("psi_elems", C.c_int64),
+        ("weight_elems", C.c_int64),
+        ("dft_points", C.c_int64),
+    ]
+
+
 SIGNATURES = {
     "pc_version": (C.c_int, []),
     "pc_create": (C.c_int, [C.POINTER(GridDesc), C.POINTER(C.c_void_p)]),
@@ -100,6 +124,27 @@ SIGNATURES = {
                                          C.POINTER(C.c_uint32)]),
     "pc_profile": (C.c_int, [C.c_void_p, C.c_int32]),
     "pc_profile_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    "pc_batch_create": (C.c_int, [C.c_int32, C.POINTER(BatchInstance), C.c_int32, C.c_double, C.c_double, C.c_double,
+                                  C.c_double, C.POINTER(C.c_void_p), C.POINTER(BatchLayout)]),
+    "pc_batch_instance_offsets": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
+    "pc_batch_bind": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "pc_batch_build_coefficients": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_double, C.c_void_p]),
+    "pc_batch_set_cpml": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double)]),
+    "pc_batch_set_sources": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32]),
+    "pc_batch_set_dft": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.c_int32, C.c_double, C.c_void_p]),
+    "pc_batch_num_variants": (C.c_int, []),
+    "pc_batch_variant_info": (C.c_int, [C.c_int32, C.POINTER(C.c_int32)]),
+    "pc_batch_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "pc_batch_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "pc_batch_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.c_void_p]),
+    "pc_batch_step": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "pc_batch_dft_flush": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "pc_batch_current_set": (C.c_int, [C.c_void_p]),
+    "pc_batch_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p]),
+    "pc_batch_launch_count": (C.c_int64, [C.c_void_p]),
+    "pc_batch_steps_done": (C.c_int64, [C.c_void_p]),
+    "pc_batch_destroy": (None, [C.c_void_p]),
 }
 
 _lock = threading.Lock()

@@ -1,0 +1,829 @@
+// Batched 2D sweep engine: many uneven 2D TE simulations (Ez, Hx, Hy: the
+// reference's "TE mode", core/solver.py:311-456 with the corrected stencil)
+// advanced together by one persistent kernel per pass.
+//
+// The reference runs a parameter sweep one design after another
+// (optimization/sweep.py:41-195, each design a full Simulation.run).  Here every
+// design of a sweep is an *instance* whose Ez/Hx/Hy live in shared device buffers
+// at per-instance offsets; a host-built work table lists (instance, tile) items,
+// LPT-sorted, and a persistent grid of CTAs walks it.
+//
+// One pass advances every instance by K steps (temporal blocking): a CTA loads
+// its tile plus a K-cell halo of Ez, Hx, Hy into shared memory, runs K leap-frog
+// steps there (the valid region shrinks by one cell per side per step), and
+// writes the tile interior to the other field set (ping-pong).  Per-cell state
+// that no neighbour reads -- Cb(Ez) and the four CPML auxiliaries -- stays in
+// registers for the whole pass.  The soft mode-profile line source is added in
+// the E phase (sources/point.py:62-73 semantics, amplitude at t_{n+1}) and the
+// port DFT lines are sampled into the shared DFT ring in the same phase.  The
+// time loop is captured once as a CUDA graph of G steps and replayed; a device
+// step counter drives the amplitude table.
+//
+// Arithmetic per point is the single-simulation 2D stepper's (stepper_split.cu
+// split_h2 / split_e2 Ez family): same operations in the same order.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "pc_internal.cuh"
+
+namespace pc {
+namespace {
+
+constexpr int BNT = 512;  // threads per CTA
+constexpr int RING_T = 16;
+
+struct BInst {  // device copy of one instance (128 bytes)
+    int nx, ny, pitch, src_x;
+    int src_y0, src_n, nport, pad0;
+    int64_t f_off, c_off, p_off, w_off;
+    int mx[4], my0[4], mn[4], mpt[4];
+};
+static_assert(sizeof(BInst) == 128, "BInst layout");
+
+struct BPass {
+    const BInst* inst;
+    const int4* items;  // (instance, x0, y0, flags)
+    int nitems;
+    const float* fin;
+    float* fout;
+    const float* cb;
+    const float* psi_in;
+    float* psi_out;
+    const float* slab;  // [3][2t]: b, a, 1/kappa by slab index
+    int t;
+    float inv_dx, inv_dy, da, db;
+    const double* amps;
+    int namps;
+    const long long* step;  // device step counter (steps completed before this chunk)
+    int s_off;              // first step of this pass relative to *step
+    int row0;               // DFT ring row of the first step of this pass
+    float* ring;
+    int npts;
+    const double* w;  // source weights
+    int live;         // 0: dry pass (no source, no sampling) used by the tuner
+};
+
+enum : unsigned {
+    F_HX = 1u,
+    F_HY = 2u,
+    F_EZ = 4u,
+    F_INT = 8u,
+    F_SRC = 16u,
+    F_PORT = 32u,
+    F_IN = 64u,
+};
+
+__device__ __forceinline__ int slab_idx(int idx, int n, int t) {
+    return idx < t ? idx : (idx >= n - t ? idx - (n - 2 * t) : 255);
+}
+
+// per-thread cells of a (TX + 2K) x (TY + 2K) region
+template <int TX, int TY, int K>
+struct BShape {
+    static constexpr int RX = TX + 2 * K, RY = TY + 2 * K, RC = RX * RY, M = (RC + BNT - 1) / BNT;
+    // two CTAs per SM (64 registers a thread) while the per-cell registers fit
+    static constexpr int MINB = M <= 6 ? 2 : 1;
+    // Ez, Hx, Hy and the four CPML auxiliaries of the region
+    static constexpr size_t SMEM = 7 * sizeof(float) * RC;
+};
+
+template <int TX, int TY, int K>
+__global__ void __launch_bounds__(BNT, BShape<TX, TY, K>::MINB) batch2d_pass(BPass P) {
+    constexpr int RX = TX + 2 * K, RY = TY + 2 * K, RC = RX * RY;
+    constexpr int M = BShape<TX, TY, K>::M;
+    extern __shared__ float smem[];
+    float* sE = smem;
+    float* sX = sE + RC;
+    float* sY = sX + RC;
+    float* qYX = sY + RC;  // psi of Hy (x-derivative)
+    float* qZX = qYX + RC; // psi of Ez (x-derivative)
+    float* qXY = qZX + RC; // psi of Hx (y-derivative)
+    float* qZY = qXY + RC; // psi of Ez (y-derivative)
+    __shared__ BInst sI;
+    const int tid = threadIdx.x;
+    const long long base = P.live ? *P.step : 0;
+    const int t = P.t;
+    const float* sb = P.slab;
+    const float* sa = P.slab + 2 * t;
+    const float* sk = P.slab + 4 * t;
+
+    for (int w = blockIdx.x; w < P.nitems; w += gridDim.x) {
+        const int4 it = P.items[w];
+        __syncthreads();  // the previous item is done with shared memory
+        if (tid < 32) reinterpret_cast<int*>(&sI)[tid] = reinterpret_cast<const int*>(P.inst + it.x)[tid];
+        __syncthreads();
+        const int nx = sI.nx, ny = sI.ny;
+        const int64_t pitch = sI.pitch;
+        const int64_t nxp = (int64_t)nx * pitch;
+        const int gx0 = it.y - K, gy0 = it.z - K;
+        const bool cp = it.w & 1;
+        const float* fin = P.fin + sI.f_off;
+        float* fout = P.fout + sI.f_off;
+        const float* cbp = P.cb + sI.c_off;
+        const int64_t pyx = sI.p_off;                                // psi Hy (x-derivative), [2t][pitch]
+        const int64_t pzx = pyx + 2 * (int64_t)t * pitch;            // psi Ez (x-derivative), [2t][pitch]
+        const int64_t pxy = pyx + 4 * (int64_t)t * pitch;            // psi Hx (y-derivative), [nx][2t]
+        const int64_t pzy = pxy + 2 * (int64_t)t * nx;               // psi Ez (y-derivative), [nx][2t]
+
+        unsigned fl[M];
+        float cbr[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            const int idx = tid + m * BNT;
+            fl[m] = 0;
+            cbr[m] = 0.f;
+            if (idx >= RC) continue;
+            const int r = idx / RY, c = idx - (idx / RY) * RY;
+            const int gi = gx0 + r, gj = gy0 + c;
+            const bool in = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
+            float e = 0.f, hx = 0.f, hy = 0.f;
+            unsigned f = 0;
+            unsigned sxs = 255, sys = 255;
+            if (in) {
+                const int64_t o = (int64_t)gi * pitch + gj;
+                e = fin[o];
+                hx = fin[nxp + o];
+                hy = fin[2 * nxp + o];
+                cbr[m] = cbp[o];
+                f |= F_IN;
+                if (c >= 1 && gi < nx - 1 && gj >= 1 && gj <= ny - 2) f |= F_HX;
+                if (r >= 1 && gi >= 1 && gi <= nx - 2 && gj < ny - 1) f |= F_HY;
+                if (r < RX - 1 && c < RY - 1 && gi < nx - 1 && gj < ny - 1) f |= F_EZ;
+                if (r >= K && r < K + TX && c >= K && c < K + TY) f |= F_INT;
+                if (gi == sI.src_x && (unsigned)(gj - sI.src_y0) < (unsigned)sI.src_n) f |= F_SRC;
+                if (f & F_INT)
+                    for (int q = 0; q < sI.nport; ++q)
+                        if (gi == sI.mx[q] && (unsigned)(gj - sI.my0[q]) < (unsigned)sI.mn[q]) f |= F_PORT;
+                if (cp) {
+                    sxs = slab_idx(gi, nx, t);
+                    sys = slab_idx(gj, ny, t);
+                    if (sxs != 255) {
+                        qYX[idx] = P.psi_in[pyx + (int64_t)sxs * pitch + gj];
+                        qZX[idx] = P.psi_in[pzx + (int64_t)sxs * pitch + gj];
+                    }
+                    if (sys != 255) {
+                        qXY[idx] = P.psi_in[pxy + (int64_t)gi * (2 * t) + sys];
+                        qZY[idx] = P.psi_in[pzy + (int64_t)gi * (2 * t) + sys];
+                    }
+                }
+            }
+            fl[m] = f | (sxs << 8) | (sys << 16);
+            sE[idx] = e;
+            sX[idx] = hx;
+            sY[idx] = hy;
+        }
+        __syncthreads();
+
+#pragma unroll
+        for (int s = 0; s < K; ++s) {
+            // H^{n+1/2} from Ez^n
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int idx = tid + m * BNT;
+                const unsigned f = fl[m];
+                if (f & F_HX) {
+                    float cy = (sE[idx] - sE[idx - 1]) * P.inv_dy;
+                    const unsigned q = (f >> 16) & 255u;
+                    if (cp && q != 255u) {
+                        const float ps = sb[q] * qXY[idx] + sa[q] * cy;
+                        qXY[idx] = ps;
+                        cy = cy * sk[q] + ps;
+                    }
+                    sX[idx] = P.da * sX[idx] - P.db * cy;
+                }
+                if (f & F_HY) {
+                    float cx = (sE[idx] - sE[idx - RY]) * P.inv_dx;
+                    const unsigned q = (f >> 8) & 255u;
+                    if (cp && q != 255u) {
+                        const float ps = sb[q] * qYX[idx] + sa[q] * cx;
+                        qYX[idx] = ps;
+                        cx = cx * sk[q] + ps;
+                    }
+                    sY[idx] = P.da * sY[idx] + P.db * cx;
+                }
+            }
+            __syncthreads();
+            // Ez^{n+1} from H^{n+1/2}, then the source at t_{n+1} and the port samples
+            double amp = 0.0;
+            if (P.live) {
+                const long long n = base + P.s_off + s;
+                if (n < P.namps) amp = P.amps[n];
+            }
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int idx = tid + m * BNT;
+                const unsigned f = fl[m];
+                if (f & F_EZ) {
+                    float c1 = (sY[idx + RY] - sY[idx]) * P.inv_dx;
+                    float c2 = (sX[idx + 1] - sX[idx]) * P.inv_dy;
+                    if (cp) {
+                        const unsigned qx = (f >> 8) & 255u, qy = (f >> 16) & 255u;
+                        if (qx != 255u) {
+                            const float ps = sb[qx] * qZX[idx] + sa[qx] * c1;
+                            qZX[idx] = ps;
+                            c1 = c1 * sk[qx] + ps;
+                        }
+                        if (qy != 255u) {
+                            const float ps = sb[qy] * qZY[idx] + sa[qy] * c2;
+                            qZY[idx] = ps;
+                            c2 = c2 * sk[qy] + ps;
+                        }
+                    }
+                    float e = sE[idx];
+                    e = e + cbr[m] * (c1 - c2);
+                    if (P.live && (f & F_SRC)) {
+                        const int gj = gy0 + (idx - (idx / RY) * RY);
+                        e = e + static_cast<float>(P.w[sI.w_off + (gj - sI.src_y0)] * amp);
+                    }
+                    sE[idx] = e;
+                    if (P.live && P.ring && (f & F_PORT)) {
+                        const int gi = gx0 + idx / RY, gj = gy0 + (idx - (idx / RY) * RY);
+                        for (int q = 0; q < sI.nport; ++q)
+                            if (gi == sI.mx[q] && (unsigned)(gj - sI.my0[q]) < (unsigned)sI.mn[q])
+                                P.ring[(int64_t)(P.row0 + s) * P.npts + sI.mpt[q] + (gj - sI.my0[q])] = e;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+
+        // tile interior -> the other set
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            const int idx = tid + m * BNT;
+            const unsigned f = fl[m];
+            if (!(f & F_INT)) continue;
+            const int gi = gx0 + idx / RY, gj = gy0 + (idx - (idx / RY) * RY);
+            const int64_t o = (int64_t)gi * pitch + gj;
+            fout[o] = sE[idx];
+            fout[nxp + o] = sX[idx];
+            fout[2 * nxp + o] = sY[idx];
+            if (cp) {
+                const unsigned qx = (f >> 8) & 255u, qy = (f >> 16) & 255u;
+                if (qx != 255u) {
+                    P.psi_out[pyx + (int64_t)qx * pitch + gj] = qYX[idx];
+                    P.psi_out[pzx + (int64_t)qx * pitch + gj] = qZX[idx];
+                }
+                if (qy != 255u) {
+                    P.psi_out[pxy + (int64_t)gi * (2 * t) + qy] = qXY[idx];
+                    P.psi_out[pzy + (int64_t)gi * (2 * t) + qy] = qZY[idx];
+                }
+            }
+        }
+    }
+}
+
+__global__ void batch_advance(long long* step, int n) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *step += n;
+}
+
+struct Variant {
+    int tx, ty, k, k1;  // tile, steps per pass, index of the K=1 sibling
+    const void* fn;
+    size_t smem;
+};
+
+#define PC_BV(TX, TY, K, K1) \
+    {TX, TY, K, K1, reinterpret_cast<const void*>(&batch2d_pass<TX, TY, K>), BShape<TX, TY, K>::SMEM}
+const Variant kVariants[] = {
+    PC_BV(32, 64, 1, 0),  PC_BV(32, 64, 2, 0),  PC_BV(32, 64, 4, 0),  PC_BV(32, 64, 8, 0),
+    PC_BV(16, 128, 1, 4), PC_BV(16, 128, 2, 4), PC_BV(16, 128, 4, 4), PC_BV(64, 64, 1, 7),
+    PC_BV(64, 64, 2, 7),  PC_BV(64, 64, 4, 7),
+};
+#undef PC_BV
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+
+}  // namespace
+}  // namespace pc
+
+using namespace pc;
+
+struct pc_batch {
+    int ninst = 0;
+    int t = 0;
+    double dx = 0, dy = 0, dt = 0, db_s = 0;
+    std::vector<pc_batch_instance> desc;
+    std::vector<BInst> inst;
+    pc_batch_layout lay{};
+    BInst* d_inst = nullptr;
+    float* d_slab = nullptr;
+    double* d_w = nullptr;
+    double* d_amps = nullptr;
+    int namps = 0;
+    long long* d_step = nullptr;
+    unsigned* d_status = nullptr;
+    float* set[2] = {nullptr, nullptr};
+    float* cb = nullptr;
+    float* psi[2] = {nullptr, nullptr};
+    bool bound = false, have_slab = false;
+    int cur = 0;
+    // DFT ports
+    bool have_dft = false;
+    DftMonitor dft{};
+    int dft_rows = 0;
+    // schedule
+    int variant = 1;
+    int graph_steps = 80;
+    int item_variant = -1;
+    int4* d_items = nullptr;
+    int nitems = 0;
+    int items_cap = 0;
+    int grid[kNumVariants] = {};
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_key[2][2] = {{-1, -1}, {-1, -1}};  // (variant, graph_steps) the graph was captured for
+    int graph_nodes[2] = {0, 0};
+    long long steps_done = 0;
+    long long launches = 0;
+};
+
+namespace pc {
+namespace {
+
+int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
+
+void drop_graphs(pc_batch* b) {
+    for (int q = 0; q < 2; ++q) {
+        if (b->graph[q]) cudaGraphExecDestroy(b->graph[q]);
+        b->graph[q] = nullptr;
+        b->graph_key[q][0] = b->graph_key[q][1] = -1;
+    }
+}
+
+// (instance, tile) items for a variant's tile shape, LPT-sorted by estimated cost
+int build_items(pc_batch* b, int v) {
+    if (b->item_variant == v) return PC_OK;
+    const Variant& V = kVariants[v];
+    std::vector<int4> items;
+    std::vector<float> cost;
+    const int t = b->t, K = V.k;
+    for (int n = 0; n < b->ninst; ++n) {
+        const int nx = b->inst[n].nx, ny = b->inst[n].ny;
+        for (int x0 = 0; x0 < nx; x0 += V.tx)
+            for (int y0 = 0; y0 < ny; y0 += V.ty) {
+                const int ax0 = x0 - K, ax1 = x0 + V.tx + K, ay0 = y0 - K, ay1 = y0 + V.ty + K;
+                const bool cp = t > 0 && (ax0 < t || ax1 > nx - t || ay0 < t || ay1 > ny - t);
+                items.push_back(make_int4(n, x0, y0, cp ? 1 : 0));
+                const int cx = std::min(nx, x0 + V.tx) - x0, cy = std::min(ny, y0 + V.ty) - y0;
+                cost.push_back((float)(cx * cy) * (cp ? 1.5f : 1.0f) + 0.25f * V.tx * V.ty);
+            }
+    }
+    if (b->d_items) drop_graphs(b);  // captured graphs hold the previous table
+    std::vector<int> ord(items.size());
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) { return cost[a] > cost[c]; });
+    std::vector<int4> sorted(items.size());
+    for (size_t q = 0; q < ord.size(); ++q) sorted[q] = items[ord[q]];
+    if ((int)sorted.size() > b->items_cap) {
+        cudaFree(b->d_items);
+        b->d_items = nullptr;
+        b->items_cap = 0;
+        PC_CUDA_CHECK(cudaMalloc(&b->d_items, sorted.size() * sizeof(int4)));
+        b->items_cap = (int)sorted.size();
+    }
+    PC_CUDA_CHECK(cudaMemcpy(b->d_items, sorted.data(), sorted.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    b->nitems = (int)sorted.size();
+    b->item_variant = v;
+    return PC_OK;
+}
+
+int grid_for(pc_batch* b, int v) {
+    if (b->grid[v] > 0) return b->grid[v];
+    int dev = 0, nsm = 0, occ = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaFuncSetAttribute(kVariants[v].fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kVariants[v].smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kVariants[v].fn, BNT, kVariants[v].smem) != cudaSuccess)
+        return -1;
+    b->grid[v] = std::max(1, nsm * std::max(1, occ));
+    return b->grid[v];
+}
+
+// A pass reads the current set and writes the other one, so a dry pass (live = 0)
+// never changes the current state.
+BPass make_pass(pc_batch* b, int s_off, int row0, bool live) {
+    BPass P{};
+    P.inst = b->d_inst;
+    P.items = b->d_items;
+    P.nitems = b->nitems;
+    const int in = b->cur, out = b->cur ^ 1;
+    P.fin = b->set[in];
+    P.fout = b->set[out];
+    P.cb = b->cb;
+    P.psi_in = b->psi[in] ? b->psi[in] : b->psi[0];
+    P.psi_out = b->psi[out] ? b->psi[out] : b->psi[0];
+    P.slab = b->d_slab;
+    P.t = b->t;
+    P.inv_dx = (float)(1.0 / b->dx);
+    P.inv_dy = (float)(1.0 / b->dy);
+    P.da = 1.0f;
+    P.db = (float)b->db_s;
+    P.amps = b->d_amps;
+    P.namps = b->namps;
+    P.step = b->d_step;
+    P.s_off = s_off;
+    P.row0 = row0;
+    P.ring = b->have_dft ? b->dft.d_ring : nullptr;
+    P.npts = b->have_dft ? b->dft.npts : 0;
+    P.w = b->d_w;
+    P.live = live ? 1 : 0;
+    return P;
+}
+
+int launch_pass(pc_batch* b, int v, const BPass& P, cudaStream_t s) {
+    const int g = grid_for(b, v);
+    if (g <= 0) return PC_ERR_CUDA;
+    const int grid = std::min(g, std::max(1, P.nitems));
+    void* args[] = {const_cast<BPass*>(&P)};
+    PC_CUDA_CHECK(cudaLaunchKernel(kVariants[v].fn, dim3(grid), dim3(BNT), args, kVariants[v].smem, s));
+    ++b->launches;
+    return PC_OK;
+}
+
+// One chunk of eager passes of variant v covering `steps` steps starting at ring row
+// b->dft_rows; flushes the DFT ring whenever it fills and advances the step counter.
+int run_passes(pc_batch* b, int v, int steps, cudaStream_t s, int* nodes) {
+    const int K = kVariants[v].k;
+    int done = 0;
+    while (done < steps) {
+        int vv = v, k = K;
+        if (steps - done < K || (b->have_dft && b->dft_rows + K > RING_T)) {
+            vv = kVariants[v].k1;
+            k = 1;
+        }
+        // the K=1 sibling reuses the table of v (same tiles; halo flags computed for K >= 1)
+        BPass P = make_pass(b, done, b->dft_rows, true);
+        int rc = launch_pass(b, vv, P, s);
+        if (rc) return rc;
+        ++*nodes;
+        b->cur ^= 1;
+        done += k;
+        if (b->have_dft) {
+            b->dft_rows += k;
+            if (b->dft_rows == RING_T) {
+                rc = launch_dft_flush_rows(b->dft, RING_T, s);
+                if (rc) return rc;
+                b->launches += 2;
+                *nodes += 2;
+                b->dft_rows = 0;
+            }
+        }
+    }
+    batch_advance<<<1, 32, 0, s>>>(b->d_step, steps);
+    PC_CUDA_CHECK(cudaGetLastError());
+    ++b->launches;
+    ++*nodes;
+    return PC_OK;
+}
+
+int ensure_graph(pc_batch* b) {
+    const int q = b->cur;
+    if (b->graph[q] && b->graph_key[q][0] == b->variant && b->graph_key[q][1] == b->graph_steps) return PC_OK;
+    if (b->graph[q]) {
+        cudaGraphExecDestroy(b->graph[q]);
+        b->graph[q] = nullptr;
+    }
+    if (!b->cap_stream) PC_CUDA_CHECK(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
+    if (grid_for(b, b->variant) <= 0 || grid_for(b, kVariants[b->variant].k1) <= 0) return PC_ERR_CUDA;
+    const int cur0 = b->cur, rows0 = b->dft_rows;
+    const long long launches0 = b->launches;
+    int nodes = 0;
+    cudaGraph_t gr = nullptr;
+    PC_CUDA_CHECK(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
+    int rc = run_passes(b, b->variant, b->graph_steps, b->cap_stream, &nodes);
+    cudaError_t e = cudaStreamEndCapture(b->cap_stream, &gr);
+    b->cur = cur0;
+    b->dft_rows = rows0;
+    b->launches = launches0;
+    if (rc) {
+        if (gr) cudaGraphDestroy(gr);
+        return rc;
+    }
+    PC_CUDA_CHECK(e);
+    e = cudaGraphInstantiate(&b->graph[q], gr, 0);
+    cudaGraphDestroy(gr);
+    PC_CUDA_CHECK(e);
+    b->graph_key[q][0] = b->variant;
+    b->graph_key[q][1] = b->graph_steps;
+    b->graph_nodes[q] = nodes;
+    return PC_OK;
+}
+
+bool graph_ok(const pc_batch* b) {
+    const int K = kVariants[b->variant].k;
+    return b->graph_steps > 0 && b->graph_steps % RING_T == 0 && (b->graph_steps / K) % 2 == 0;
+}
+
+}  // namespace
+}  // namespace pc
+
+extern "C" {
+
+int pc_batch_create(int32_t ninst, const pc_batch_instance* desc, int32_t cpml_t, double dx, double dy, double dt,
+                    double db_s, pc_batch** out, pc_batch_layout* lay) {
+    if (!out || !lay || ninst <= 0 || !desc || cpml_t < 0 || cpml_t > 100 || !(dx > 0) || !(dy > 0) || !(dt > 0))
+        return PC_ERR_INVALID;
+    *out = nullptr;
+    pc_batch* b = new pc_batch();
+    b->ninst = ninst;
+    b->t = cpml_t;
+    b->dx = dx;
+    b->dy = dy;
+    b->dt = dt;
+    b->db_s = db_s;
+    b->desc.assign(desc, desc + ninst);
+    int64_t foff = 0, coff = 0, poff = 0, woff = 0, pts = 0;
+    for (int n = 0; n < ninst; ++n) {
+        const pc_batch_instance& d = desc[n];
+        if (d.nx < 2 * cpml_t + 4 || d.ny < 2 * cpml_t + 4 || d.nx > (1 << 20) || d.ny > (1 << 20) || d.nport < 0 ||
+            d.nport > 4 || d.src_n < 0 || d.src_x < 0 || d.src_x >= d.nx - 1 || d.src_y0 < 0 ||
+            d.src_y0 + d.src_n > d.ny - 1) {
+            delete b;
+            return PC_ERR_INVALID;
+        }
+        BInst I{};
+        I.nx = d.nx;
+        I.ny = d.ny;
+        I.pitch = (int)round_up(d.ny, 32);
+        I.src_x = d.src_x;
+        I.src_y0 = d.src_y0;
+        I.src_n = d.src_n;
+        I.nport = d.nport;
+        I.f_off = foff;
+        I.c_off = coff;
+        I.p_off = poff;
+        I.w_off = woff;
+        for (int q = 0; q < 4; ++q) I.mx[q] = I.my0[q] = I.mn[q] = I.mpt[q] = 0;
+        for (int q = 0; q < d.nport; ++q) {
+            if (d.port_x[q] < 0 || d.port_x[q] >= d.nx - 1 || d.port_y0[q] < 0 || d.port_n[q] <= 0 ||
+                d.port_y0[q] + d.port_n[q] > d.ny - 1) {
+                delete b;
+                return PC_ERR_INVALID;
+            }
+            I.mx[q] = d.port_x[q];
+            I.my0[q] = d.port_y0[q];
+            I.mn[q] = d.port_n[q];
+            I.mpt[q] = (int)pts;
+            pts += d.port_n[q];
+        }
+        const int64_t plane = (int64_t)d.nx * I.pitch;
+        foff += 3 * plane;
+        coff += plane;
+        poff += 4 * (int64_t)cpml_t * (I.pitch + d.nx);
+        woff += d.src_n;
+        b->inst.push_back(I);
+    }
+    b->lay.field_elems = foff;
+    b->lay.coef_elems = coff;
+    b->lay.psi_elems = std::max<int64_t>(poff, 1);
+    b->lay.weight_elems = woff;
+    b->lay.dft_points = pts;
+    *lay = b->lay;
+    bool ok = cudaMalloc(&b->d_inst, ninst * sizeof(BInst)) == cudaSuccess &&
+              cudaMalloc(&b->d_step, sizeof(long long)) == cudaSuccess &&
+              cudaMalloc(&b->d_status, sizeof(unsigned)) == cudaSuccess &&
+              cudaMalloc(&b->d_w, std::max<int64_t>(woff, 1) * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&b->d_slab, std::max(1, 6 * cpml_t) * sizeof(float)) == cudaSuccess;
+    ok = ok && cudaMemcpy(b->d_inst, b->inst.data(), ninst * sizeof(BInst), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemset(b->d_step, 0, sizeof(long long)) == cudaSuccess &&
+         cudaMemset(b->d_status, 0, sizeof(unsigned)) == cudaSuccess &&
+         cudaMemset(b->d_w, 0, std::max<int64_t>(woff, 1) * sizeof(double)) == cudaSuccess;
+    if (!ok) {
+        pc_batch_destroy(b);
+        return PC_ERR_CUDA;
+    }
+    b->have_slab = cpml_t == 0;
+    *out = b;
+    return PC_OK;
+}
+
+int pc_batch_instance_offsets(const pc_batch* b, int32_t i, int64_t out[5]) {
+    if (!b || !out || i < 0 || i >= b->ninst) return PC_ERR_INVALID;
+    const BInst& I = b->inst[i];
+    out[0] = I.f_off;
+    out[1] = I.pitch;
+    out[2] = I.c_off;
+    out[3] = I.w_off;
+    out[4] = I.nport ? I.mpt[0] : -1;
+    return PC_OK;
+}
+
+int pc_batch_bind(pc_batch* b, void* d_set0, void* d_set1, void* d_cb, void* d_psi0, void* d_psi1) {
+    if (!b || !d_set0 || !d_set1 || !d_cb || d_set0 == d_set1) return PC_ERR_INVALID;
+    if (b->t > 0 && (!d_psi0 || !d_psi1 || d_psi0 == d_psi1)) return PC_ERR_INVALID;
+    b->set[0] = static_cast<float*>(d_set0);
+    b->set[1] = static_cast<float*>(d_set1);
+    b->cb = static_cast<float*>(d_cb);
+    b->psi[0] = static_cast<float*>(d_psi0);
+    b->psi[1] = static_cast<float*>(d_psi1);
+    b->cur = 0;
+    b->bound = true;
+    drop_graphs(b);
+    return PC_OK;
+}
+
+int pc_batch_build_coefficients(pc_batch* b, int32_t i, const double* d_eps, double eps0, void* stream) {
+    if (!b || !b->bound || i < 0 || i >= b->ninst || !d_eps || !(eps0 > 0)) return PC_ERR_INVALID;
+    const BInst& I = b->inst[i];
+    pc_grid_desc g{};
+    g.ndim = 2;
+    g.nx = I.nx;
+    g.ny = I.ny;
+    g.nz = 1;
+    g.pitch = I.pitch;
+    g.precision = 4;
+    g.dt = b->dt;
+    void* cb[3] = {nullptr, nullptr, b->cb + I.c_off};
+    int64_t l = 0;
+    int rc = launch_build_coefficients(g, d_eps, nullptr, nullptr, nullptr, eps0, 1.0, nullptr, cb, nullptr, nullptr,
+                                       (cudaStream_t)stream, &l);
+    b->launches += l;
+    return rc;
+}
+
+int pc_batch_set_cpml(pc_batch* b, const double* bcoef, const double* acoef, const double* kappa) {
+    if (!b || b->t <= 0 || !bcoef || !acoef || !kappa) return PC_ERR_INVALID;
+    const int t2 = 2 * b->t;
+    std::vector<float> h(3 * t2);
+    for (int q = 0; q < t2; ++q) {
+        if (!(kappa[q] > 0)) return PC_ERR_INVALID;
+        h[q] = (float)bcoef[q];
+        h[t2 + q] = (float)acoef[q];
+        h[2 * t2 + q] = (float)(1.0 / kappa[q]);
+    }
+    PC_CUDA_CHECK(cudaMemcpy(b->d_slab, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    b->have_slab = true;
+    return PC_OK;
+}
+
+int pc_batch_set_sources(pc_batch* b, const double* weights, const double* amps, int32_t namps) {
+    if (!b || namps < 0 || (namps > 0 && !amps) || (b->lay.weight_elems > 0 && !weights)) return PC_ERR_INVALID;
+    if (b->lay.weight_elems > 0)
+        PC_CUDA_CHECK(cudaMemcpy(b->d_w, weights, b->lay.weight_elems * sizeof(double), cudaMemcpyHostToDevice));
+    if (namps > b->namps || !b->d_amps) {
+        cudaFree(b->d_amps);
+        b->d_amps = nullptr;
+        PC_CUDA_CHECK(cudaMalloc(&b->d_amps, std::max(1, namps) * sizeof(double)));
+    }
+    if (namps > 0) PC_CUDA_CHECK(cudaMemcpy(b->d_amps, amps, namps * sizeof(double), cudaMemcpyHostToDevice));
+    b->namps = namps;
+    return PC_OK;
+}
+
+int pc_batch_set_dft(pc_batch* b, const double* omega, int32_t nf, double t0, void* d_acc) {
+    if (!b || b->have_dft || b->lay.dft_points <= 0 || b->lay.dft_points > INT32_MAX) return PC_ERR_INVALID;
+    std::vector<int64_t> offs(b->lay.dft_points);
+    for (const BInst& I : b->inst)
+        for (int q = 0; q < I.nport; ++q)
+            for (int y = 0; y < I.mn[q]; ++y)
+                offs[I.mpt[q] + y] = I.f_off + (int64_t)I.mx[q] * I.pitch + I.my0[q] + y;
+    const int rc = dft_monitor_init(b->dft, 2, offs.data(), (int)offs.size(), omega, nf, b->dt, t0, d_acc,
+                                    b->lay.field_elems);
+    if (rc) return rc;
+    b->have_dft = true;
+    b->dft_rows = 0;
+    drop_graphs(b);
+    return PC_OK;
+}
+
+int pc_batch_num_variants(void) { return kNumVariants; }
+
+int pc_batch_variant_info(int32_t v, int32_t out[3]) {
+    if (v < 0 || v >= kNumVariants || !out) return PC_ERR_INVALID;
+    out[0] = kVariants[v].tx;
+    out[1] = kVariants[v].ty;
+    out[2] = kVariants[v].k;
+    return PC_OK;
+}
+
+int pc_batch_set_tuning(pc_batch* b, int32_t variant, int32_t graph_steps) {
+    if (!b || variant < 0 || variant >= kNumVariants || graph_steps < 0) return PC_ERR_INVALID;
+    const int old_v = b->variant, old_g = b->graph_steps;
+    b->variant = variant;
+    b->graph_steps = graph_steps;
+    if (graph_steps > 0 && !graph_ok(b)) {
+        b->variant = old_v;
+        b->graph_steps = old_g;
+        return PC_ERR_INVALID;
+    }
+    return PC_OK;
+}
+
+int pc_batch_get_tuning(const pc_batch* b, int32_t* variant, int32_t* graph_steps) {
+    if (!b || !variant || !graph_steps) return PC_ERR_INVALID;
+    *variant = b->variant;
+    *graph_steps = b->graph_steps;
+    return PC_OK;
+}
+
+int pc_batch_autotune(pc_batch* b, int32_t passes, float* ms_per_step, void* stream) {
+    if (!b || !b->bound || passes <= 0 || (b->t > 0 && !b->have_slab)) return PC_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaEvent_t e0, e1;
+    PC_CUDA_CHECK(cudaEventCreate(&e0));
+    PC_CUDA_CHECK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bestv = b->variant;
+    for (int v = 0; v < kNumVariants; ++v) {
+        int rc = build_items(b, v);
+        if (rc) return rc;
+        BPass P = make_pass(b, 0, 0, false);
+        rc = launch_pass(b, v, P, s);  // warm-up
+        if (rc) return rc;
+        PC_CUDA_CHECK(cudaEventRecord(e0, s));
+        for (int q = 0; q < passes; ++q) {
+            rc = launch_pass(b, v, P, s);
+            if (rc) return rc;
+        }
+        PC_CUDA_CHECK(cudaEventRecord(e1, s));
+        PC_CUDA_CHECK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        PC_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+        const float per_step = ms / (passes * kVariants[v].k);
+        if (ms_per_step) ms_per_step[v] = per_step;
+        if (per_step < best) {
+            best = per_step;
+            bestv = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->variant = bestv;
+    if (b->graph_steps > 0 && !graph_ok(b)) b->graph_steps = 16 * 2 * kVariants[bestv].k;
+    return PC_OK;
+}
+
+int pc_batch_step(pc_batch* b, int32_t nsteps, void* stream) {
+    if (!b || nsteps < 0) return PC_ERR_INVALID;
+    if (!b->bound || (b->t > 0 && !b->have_slab)) return PC_ERR_STATE;
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = build_items(b, b->variant);
+    if (rc) return rc;
+    const bool use_graph = b->graph_steps > 0 && graph_ok(b);
+    while (nsteps > 0) {
+        if (use_graph && b->dft_rows == 0 && nsteps >= b->graph_steps) {
+            rc = ensure_graph(b);
+            if (rc) return rc;
+            PC_CUDA_CHECK(cudaGraphLaunch(b->graph[b->cur], s));
+            b->launches += b->graph_nodes[b->cur];
+            b->steps_done += b->graph_steps;
+            nsteps -= b->graph_steps;
+            continue;  // an even number of passes: the current set is unchanged
+        }
+        // eager passes up to the next ring boundary (or the end)
+        int chunk = nsteps;
+        if (b->have_dft) chunk = std::min(chunk, RING_T - b->dft_rows);
+        int nodes = 0;
+        rc = run_passes(b, b->variant, chunk, s, &nodes);
+        if (rc) return rc;
+        b->steps_done += chunk;
+        nsteps -= chunk;
+    }
+    return PC_OK;
+}
+
+int pc_batch_dft_flush(pc_batch* b, void* stream) {
+    if (!b) return PC_ERR_INVALID;
+    if (!b->have_dft || b->dft_rows == 0) return PC_OK;
+    const int rc = launch_dft_flush_rows(b->dft, b->dft_rows, (cudaStream_t)stream);
+    if (rc) return rc;
+    b->launches += 2;
+    b->dft_rows = 0;
+    return PC_OK;
+}
+
+int pc_batch_current_set(const pc_batch* b) { return b ? b->cur : PC_ERR_INVALID; }
+
+int pc_batch_status(pc_batch* b, uint32_t* flags, void* stream) {
+    if (!b || !flags) return PC_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned v = 0;
+    PC_CUDA_CHECK(cudaMemcpyAsync(&v, b->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    PC_CUDA_CHECK(cudaStreamSynchronize(s));
+    *flags = v;
+    return PC_OK;
+}
+
+int64_t pc_batch_launch_count(const pc_batch* b) { return b ? b->launches : PC_ERR_INVALID; }
+
+int64_t pc_batch_steps_done(const pc_batch* b) { return b ? b->steps_done : PC_ERR_INVALID; }
+
+void pc_batch_destroy(pc_batch* b) {
+    if (!b) return;
+    drop_graphs(b);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    if (b->have_dft) dft_monitor_free(b->dft);
+    cudaFree(b->d_inst);
+    cudaFree(b->d_slab);
+    cudaFree(b->d_w);
+    cudaFree(b->d_amps);
+    cudaFree(b->d_step);
+    cudaFree(b->d_status);
+    cudaFree(b->d_items);
+    delete b;
+}
+
+}  // extern "C"

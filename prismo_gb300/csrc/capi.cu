@@ -34,6 +34,54 @@ PsiLayout psi_layout(const pc_grid_desc& g, int t) {
     return L;
 }
 
+int dft_monitor_init(DftMonitor& m, int comp, const int64_t* offsets, int npts, const double* omega, int nf, double dt,
+                     double t0, void* d_acc, int64_t limit) {
+    if (npts <= 0 || !offsets || !omega || nf <= 0 || !(dt > 0) || !d_acc) return PC_ERR_INVALID;
+    for (int i = 0; i < npts; ++i)
+        if (offsets[i] < 0 || offsets[i] >= limit) return PC_ERR_INVALID;
+    m = DftMonitor{};
+    m.comp = comp;
+    m.npts = npts;
+    m.nf = nf;
+    m.T = 16;
+    m.dt = dt;
+    m.d_acc = static_cast<float4*>(d_acc);
+    std::vector<double> st(2 * nf), rot(2 * nf);
+    for (int f = 0; f < nf; ++f) {
+        // phase of the first sample, t0 = t_{n+1} of the next step, and one-step rotation
+        st[2 * f] = cos(-omega[f] * t0);
+        st[2 * f + 1] = sin(-omega[f] * t0);
+        rot[2 * f] = cos(-omega[f] * dt);
+        rot[2 * f + 1] = sin(-omega[f] * dt);
+    }
+    bool ok = cudaMalloc(&m.d_off, npts * sizeof(int64_t)) == cudaSuccess &&
+              cudaMalloc(&m.d_ring, (size_t)m.T * npts * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&m.d_table, (size_t)m.T * nf * sizeof(float2)) == cudaSuccess &&
+              cudaMalloc(&m.d_state, nf * sizeof(double2)) == cudaSuccess &&
+              cudaMalloc(&m.d_rot, nf * sizeof(double2)) == cudaSuccess;
+    ok = ok && cudaMemcpy(m.d_off, offsets, npts * sizeof(int64_t), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(m.d_state, st.data(), nf * sizeof(double2), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(m.d_rot, rot.data(), nf * sizeof(double2), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (!ok) {
+        dft_monitor_free(m);
+        return PC_ERR_CUDA;
+    }
+    return PC_OK;
+}
+
+void dft_monitor_free(DftMonitor& m) {
+    cudaFree(m.d_off);
+    cudaFree(m.d_ring);
+    cudaFree(m.d_table);
+    cudaFree(m.d_state);
+    cudaFree(m.d_rot);
+    m.d_off = nullptr;
+    m.d_ring = nullptr;
+    m.d_table = nullptr;
+    m.d_state = nullptr;
+    m.d_rot = nullptr;
+}
+
 }  // namespace pc
 
 using namespace pc;
@@ -92,13 +140,7 @@ void pc_destroy(pc_ctx* c) {
         cudaFree(s.d_off);
         cudaFree(s.d_w);
     }
-    for (auto& m : c->dfts) {
-        cudaFree(m.d_off);
-        cudaFree(m.d_ring);
-        cudaFree(m.d_table);
-        cudaFree(m.d_state);
-        cudaFree(m.d_rot);
-    }
+    for (auto& m : c->dfts) dft_monitor_free(m);
     cudaFree(c->d_amps);
     cudaFree(c->d_cpml_coef);
     cudaFree(c->d_cpml_slab);
@@ -321,42 +363,11 @@ int pc_step(pc_ctx* c, int32_t nsteps, const double* amps, void* stream) {
 
 int pc_add_dft(pc_ctx* c, int32_t comp, const int64_t* offsets, int32_t npts, const double* omega, int32_t nf,
                double dt, double t0, void* d_acc) {
-    if (!c || comp < 0 || comp > 5 || npts <= 0 || !offsets || !omega || nf <= 0 || !(dt > 0) || !d_acc)
-        return PC_ERR_INVALID;
-    const int64_t lim = (int64_t)c->g.nx * c->g.ny * c->g.pitch;
-    for (int i = 0; i < npts; ++i)
-        if (offsets[i] < 0 || offsets[i] >= lim) return PC_ERR_INVALID;
+    if (!c || comp < 0 || comp > 5) return PC_ERR_INVALID;
     DftMonitor m{};
-    m.comp = comp;
-    m.npts = npts;
-    m.nf = nf;
-    m.T = 16;
-    m.dt = dt;
-    m.d_acc = static_cast<float4*>(d_acc);
-    std::vector<double> st(2 * nf), rot(2 * nf);
-    for (int f = 0; f < nf; ++f) {
-        // phase of the first sample, t0 = t_{n+1} of the next step, and one-step rotation
-        st[2 * f] = cos(-omega[f] * t0);
-        st[2 * f + 1] = sin(-omega[f] * t0);
-        rot[2 * f] = cos(-omega[f] * dt);
-        rot[2 * f + 1] = sin(-omega[f] * dt);
-    }
-    bool ok = cudaMalloc(&m.d_off, npts * sizeof(int64_t)) == cudaSuccess &&
-              cudaMalloc(&m.d_ring, (size_t)m.T * npts * sizeof(float)) == cudaSuccess &&
-              cudaMalloc(&m.d_table, (size_t)m.T * nf * sizeof(float2)) == cudaSuccess &&
-              cudaMalloc(&m.d_state, nf * sizeof(double2)) == cudaSuccess &&
-              cudaMalloc(&m.d_rot, nf * sizeof(double2)) == cudaSuccess;
-    ok = ok && cudaMemcpy(m.d_off, offsets, npts * sizeof(int64_t), cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemcpy(m.d_state, st.data(), nf * sizeof(double2), cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemcpy(m.d_rot, rot.data(), nf * sizeof(double2), cudaMemcpyHostToDevice) == cudaSuccess;
-    if (!ok) {
-        cudaFree(m.d_off);
-        cudaFree(m.d_ring);
-        cudaFree(m.d_table);
-        cudaFree(m.d_state);
-        cudaFree(m.d_rot);
-        return PC_ERR_CUDA;
-    }
+    const int rc = dft_monitor_init(m, comp, offsets, npts, omega, nf, dt, t0, d_acc,
+                                    (int64_t)c->g.nx * c->g.ny * c->g.pitch);
+    if (rc) return rc;
     c->dfts.push_back(m);
     return (int)c->dfts.size() - 1;
 }

@@ -70,6 +70,23 @@ __global__ void dft_flush(const float* __restrict__ ring, int npts, int rows, co
 
 }  // namespace
 
+// launch helpers shared with the batched sweep (batch.cu)
+int launch_dft_sample_f32(const float* field, DftMonitor& m, int row, cudaStream_t s) {
+    const int threads = 256;
+    const int blocks = (m.npts + threads - 1) / threads < 1024 ? (m.npts + threads - 1) / threads : 1024;
+    dft_sample<float><<<blocks, threads, 0, s>>>(field, m.d_off, m.npts, m.d_ring, row);
+    PC_CUDA_CHECK(cudaGetLastError());
+    return PC_OK;
+}
+
+int launch_dft_flush_rows(DftMonitor& m, int rows, cudaStream_t s) {
+    dft_phase<<<(m.nf + 127) / 128, 128, 0, s>>>(m.d_state, m.d_rot, m.nf, rows, m.d_table);
+    dim3 grd((m.npts + 255) / 256, m.nf);
+    dft_flush<<<grd, 256, 0, s>>>(m.d_ring, m.npts, rows, m.d_table, m.nf, (float)m.dt, m.d_acc);
+    PC_CUDA_CHECK(cudaGetLastError());
+    return PC_OK;
+}
+
 int dft_after_step(pc_ctx* c, cudaStream_t s) {
     for (auto& m : c->dfts) {
         const int threads = 256;

@@ -169,6 +169,11 @@ int launch_sources(pc_ctx* c, int step_in_batch, cudaStream_t s);
 int launch_fused_step(pc_ctx* c, cudaStream_t s);
 void destroy_fused_state(pc_ctx* c);
 int dft_after_step(pc_ctx* c, cudaStream_t s);
+int launch_dft_sample_f32(const float* field, DftMonitor& m, int row, cudaStream_t s);
+int launch_dft_flush_rows(DftMonitor& m, int rows, cudaStream_t s);
+int dft_monitor_init(DftMonitor& m, int comp, const int64_t* offsets, int npts, const double* omega, int nf, double dt,
+                     double t0, void* d_acc, int64_t limit);
+void dft_monitor_free(DftMonitor& m);
 int dft_flush_monitor(pc_ctx* c, DftMonitor& m, cudaStream_t s);
 
 }  // namespace pc

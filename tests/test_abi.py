@@ -73,3 +73,25 @@ def test_error_mapping():
     with pytest.raises(FloatingPointError):
         _lib.check(_lib.PC_ERR_NONFINITE, "x")
     assert _lib.check(3) == 3
+
+
+def test_batch_create_rejects_bad_instances_without_gpu(lib):
+    """Instance validation happens before any CUDA call."""
+    from prismo_gb300 import _lib
+
+    inst = (_lib.BatchInstance * 1)()
+    inst[0].nx, inst[0].ny = 30, 30  # too small for a 20-cell CPML
+    inst[0].src_x, inst[0].src_y0, inst[0].src_n = 5, 5, 4
+    h = ctypes.c_void_p()
+    lay = _lib.BatchLayout()
+    assert lib.pc_batch_create(1, inst, 20, 2e-8, 2e-8, 1e-17, 1e-11, ctypes.byref(h), ctypes.byref(lay)) \
+        == _lib.PC_ERR_INVALID
+    inst[0].nx, inst[0].ny = 100, 100
+    inst[0].nport = 1
+    inst[0].port_x[0], inst[0].port_y0[0], inst[0].port_n[0] = 50, 95, 10  # runs past the Ez extent
+    assert lib.pc_batch_create(1, inst, 20, 2e-8, 2e-8, 1e-17, 1e-11, ctypes.byref(h), ctypes.byref(lay)) \
+        == _lib.PC_ERR_INVALID
+    assert lib.pc_batch_num_variants() >= 4
+    out = (ctypes.c_int32 * 3)()
+    assert lib.pc_batch_variant_info(0, out) == 0 and out[2] == 1
+    assert lib.pc_batch_variant_info(99, out) == _lib.PC_ERR_INVALID
