@@ -2,6 +2,7 @@
 benchmark = one whole 2000-time-step simulation from zero fields).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py --workload dispersive|sweep|surrogate   (the other configurations)
 
 Workload (the reference's 3D plain-FDTD configuration): 256^3 total cells at
 dx = 20 nm with a 12-cell CPML on all six faces, Courant 0.5, 32 seeded
@@ -224,7 +225,13 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--dims", type=int, default=None,
                     help="cube edge for a reduced profiling case (default: the 256^3 workload)")
+    ap.add_argument("--workload", default="3d", choices=["3d", "dispersive", "sweep", "surrogate"],
+                    help="3d: the headline 256^3 CPML workload; dispersive: 384x384x192 Drude-Lorentz + TFSF + "
+                         "64-frequency DFT planes; sweep: 64 batched couplers; surrogate: train + held-out pipeline")
+    ap.add_argument("--designs", type=int, default=64, help="designs per batched sweep")
     args = ap.parse_args()
+    if args.workload != "3d":
+        return run_other(args)
     global DIMS
     if args.dims:
         DIMS = (args.dims,) * 3
@@ -363,6 +370,201 @@ def run_e2e(eng, eps, amps, tsteps, cells, reps=2):
     ms = ev0.elapsed_time(ev1) / reps
     return {"value": cells * tsteps / (ms / 1e3) / 1e9, "unit": "Gcell/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "ms_per_step": ms, "api": "prismo_gb300.engine.FDTDEngine (host eps in, host fields out)"}
+
+
+# ---------------------------------------------------------------------------
+# the other configurations (run by hand: python bench.py --workload ...)
+# ---------------------------------------------------------------------------
+def _line(**kw):
+    base = {"n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic"}
+    base.update(kw)
+    print(json.dumps(base), flush=True)
+
+
+def _oracle_coupler_worker(seed, nsteps):
+    """One design's coupler + normalisation run on the float64 oracle, nsteps of
+    the 4000 (a bounded sample); returns seconds per 4000-step design."""
+    from oracle import fdtd64 as O
+    from prismo_gb300 import sweep as S
+
+    L = S.coupler_layout(S.coupler_design(seed))
+    el = 0.0
+    for eps, ports in ((L.eps, L.ports), (L.norm_eps, L.ports[:1])):
+        nx, ny = eps.shape
+        g = O.OracleGrid.from_total(nx, ny, 1, S.DX, S.CPML)
+        o = O.OracleFDTD(g, S.sweep_dt(), {"eps_rel": eps[:, :, None]}, cpml_layers=S.CPML)
+        o.add_source("Ez", (np.array([[L.src.x]]), np.arange(L.src.y0, L.src.y0 + L.src.n)[None, :]),
+                     O.gaussian_pulse(S.F0, S.PULSE_WIDTH), weight=L.src.profile[None, :])
+        for p in ports:
+            o.add_dft("Ez", (np.array([[p.x]]), np.arange(p.y0, p.y0 + p.n)[None, :]), S.sweep_freqs(S.NFREQ))
+        o.step()
+        t0 = time.perf_counter()
+        for _ in range(nsteps):
+            o.step()
+        el += (time.perf_counter() - t0) / nsteps * S.STEPS
+    return el
+
+
+def sweep_cpu_baseline(nsteps=10):
+    """ParameterSweep(parallel=True) shape: one float64 oracle design per host core."""
+    import multiprocessing as mp
+
+    cores = os.cpu_count() or 1
+    with mp.get_context("spawn").Pool(cores) as pool:
+        secs = pool.starmap(_oracle_coupler_worker, [(s, nsteps) for s in range(cores)])
+    return sum(1.0 / x for x in secs), cores, float(np.mean(secs))
+
+
+def run_other(args):
+    if args.workload == "sweep" or args.workload == "surrogate":
+        cpu = None
+        if not args.no_cpu_baseline:  # before any GPU work: the pool is spawned
+            v, cores, sec = sweep_cpu_baseline()
+            cpu = {"value": v, "unit": "designs/s", "cores": cores, "kind": "port",
+                   "sample": f"10 of 4000 steps of one coupler + normalisation per core, float64 oracle "
+                             f"(ParameterSweep parallel shape), {sec:.0f} s per design extrapolated"}
+    import torch
+
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    peak, peak_kind = measured_peaks()
+    if args.workload == "dispersive":
+        return run_dispersive(args, peak, peak_kind)
+    if args.workload == "sweep":
+        return run_sweep(args, cpu, peak, peak_kind)
+    return run_surrogate(args, cpu)
+
+
+def run_dispersive(args, peak, peak_kind):
+    """384x384x192 Drude + 2 Lorentz metal, ridge, TFSF, two 64-frequency DFT
+    planes; each bench step continues the simulation by --tsteps (default 400)
+    time steps (warm-up + timed steps stay within the 4000-step run)."""
+    import torch
+
+    from prismo_gb300.workloads import CONFIG_3D_DISPERSIVE, build_dispersive_engine, dispersive_bytes_per_cell
+
+    dims = CONFIG_3D_DISPERSIVE["dims"]
+    per = args.tsteps if args.tsteps != TSTEPS else 400
+    eng, info = build_dispersive_engine(dims)
+    total = (args.warmup + args.steps) * per
+    amps = info["waveform"]((np.arange(total) + 1) * info["dt"])[:, None]
+    pos = 0
+
+    def one():
+        nonlocal pos
+        eng.step(per, amps[pos:pos + per])
+        pos += per
+
+    for _ in range(args.warmup):
+        one()
+    eng.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    n0 = eng.launch_count()
+    eng.profile(True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(eng.stream)
+    for _ in range(args.steps):
+        one()
+    ev1.record(eng.stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    kern_ms, kern_n = eng.profile_read()
+    clk = clocks.stop()
+    status = eng.check_status()
+    cells = float(np.prod(dims))
+    value = cells * per * args.steps / (ms / 1e3) / 1e9
+    bpc = dispersive_bytes_per_cell(dims, 12, info["box"], 2, len(info["planes"]), len(info["freqs"]))
+    avg = kern_ms / 1e3 / max(kern_n, 1)
+    ach = bpc * cells / avg / 1e9
+    _line(metric="Gcell-updates/s", value=value, unit="Gcell/s", steps=args.steps, warmup=args.warmup,
+          ms_per_step=ms / args.steps, dtype="f32",
+          config={"workload": "3d_dispersive_384x384x192: Drude + 2 Lorentz half-space metal, Si3N4 ridge, TFSF "
+                              "plane wave (-z, Ex), two 64-frequency Ex DFT planes, 12-cell CPML",
+                  "time_steps_per_step": per, "status": status, "l2": "inputs larger than L2"},
+          roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                    "peak_kind": peak_kind, "traffic": None, "bytes_per_cell_update": bpc,
+                    "kernel": "split H + E(ADE) + TFSF stencil per step", "avg_launch_us": avg * 1e6},
+          gpu_launches=eng.launch_count() - n0, clocks=clk)
+    eng.close()
+
+
+def run_sweep(args, cpu, peak, peak_kind):
+    """Batched coupler sweep: one bench step = --designs designs x 4000 steps."""
+    import torch
+
+    from prismo_gb300 import sweep as S
+
+    designs = [S.coupler_design(s) for s in range(args.designs)]
+    layouts = [S.coupler_layout(d) for d in designs]
+    B = S.BatchedFDTD2D(S.instances_for(layouts), S.sweep_freqs(S.NFREQ))
+    variant = B.tuning()[0]
+    tile = S.BatchedFDTD2D.variants()[variant]
+    cells = sum(I.eps.shape[0] * I.eps.shape[1] for I in B.instances)
+    B.close()
+    runs = []
+    for q in range(max(args.warmup, 3) + args.steps):
+        r = S.batched_sweep(designs, layouts=layouts, variant=variant)
+        runs.append(r)
+    timed = runs[-args.steps:]
+    run_s = sum(r.run_seconds for r in timed) / args.steps
+    e2e_s = sum(r.seconds for r in timed) / args.steps
+    # end to end from the design list (layouts included) once more
+    e2e = S.batched_sweep(designs, variant=variant)
+    ser = S.serial_sweep(designs[:2])
+    err = float(np.abs(timed[-1].S[:2] - ser.S).max())
+    # the batch kernel's roofline: unblocked 2D bytes per cell update (28 B + CPML edges)
+    bpc = 28.0 + 16.0 * float(np.mean([(2 * S.CPML / I.eps.shape[0] + 2 * S.CPML / I.eps.shape[1])
+                                       for I in S.instances_for(layouts)]))
+    gcell = cells * S.STEPS / run_s / 1e9
+    ach = gcell * bpc
+    _line(metric="designs/s", value=args.designs / run_s, unit="designs/s", steps=args.steps, warmup=args.warmup,
+          ms_per_step=run_s * 1e3, dtype="f32",
+          config={"workload": f"batched 2D coupler sweep: {args.designs} designs (seeds 0..{args.designs - 1}), "
+                              "Nx 400-1200, Ny 200-800, 20-cell CPML, 4000 steps, 4 ports x 64 frequencies, "
+                              "plus one normalisation run per design",
+                  "variant_tile_steps": tile, "gcell_per_s": gcell, "l2": "inputs larger than L2"},
+          e2e={"value": args.designs / e2e.seconds, "unit": "designs/s", "h2d_bytes_per_step": int(
+              sum(I.eps.nbytes for I in S.instances_for(layouts))), "d2h_bytes_per_step": int(
+              e2e.S.size * 16), "api": "prismo_gb300.sweep.batched_sweep (design list in, S-parameters out)"},
+          serial_designs_per_s=ser.designs_per_s, batched_vs_serial=(args.designs / e2e.seconds) / ser.designs_per_s,
+          max_abs_S_batched_vs_serial=err,
+          roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                    "peak_kind": peak_kind, "traffic": None, "bytes_per_cell_update": bpc,
+                    "kernel": f"batch2d_pass<{tile[0]},{tile[1]},{tile[2]}> (unblocked bytes; K steps per pass)"},
+          cpu_baseline=cpu, gpu_launches=timed[-1].launches)
+
+
+def run_surrogate(args, cpu):
+    """Train the 4-member ensemble on 4096 batched-FDTD designs, then run the
+    surrogate + FDTD-fallback pipeline on 256 held-out designs."""
+    import torch
+
+    from prismo_gb300 import surrogate as Su
+    from prismo_gb300 import sweep as S
+
+    t0 = time.perf_counter()
+    train = [S.coupler_design(s) for s in range(4096)]
+    test = [S.coupler_design(s) for s in range(10000, 10256)]
+    Str = np.concatenate([S.batched_sweep(train[q:q + 1024]).S for q in range(0, 4096, 1024)])
+    ref = S.batched_sweep(test)
+    t_data = time.perf_counter() - t0
+    E = Su.Ensemble()
+    E.fit(train, Str, epochs=Su.EPOCHS)
+    res = Su.run_pipeline(E, test)
+    err = Su.s_error(res.S, ref.S)
+    ser = S.serial_sweep(test[:2])
+    _line(metric="designs/s", value=res.designs_per_s, unit="designs/s", steps=1, warmup=0,
+          ms_per_step=res.seconds * 1e3, dtype="bf16 (f32 accumulate)",
+          config={"workload": "surrogate + batched-FDTD fallback on 256 held-out couplers (seeds 10000-10255); "
+                              "4-member ensemble 3-256-256-256-512 SiLU trained on 4096 designs",
+                  "threshold": Su.THRESHOLD, "train_seconds": E.train_seconds, "data_seconds": t_data},
+          accepted=int(res.accepted.sum()), err_rms_max=float(err.max()), err_rms_median=float(np.median(err)),
+          batched_fdtd_designs_per_s=len(test) / ref.seconds, serial_designs_per_s=ser.designs_per_s,
+          pipeline_vs_serial=res.designs_per_s / ser.designs_per_s,
+          e2e={"value": res.designs_per_s, "unit": "designs/s", "h2d_bytes_per_step": len(test) * 12,
+               "d2h_bytes_per_step": len(test) * 512 * 4, "api": "prismo_gb300.surrogate.run_pipeline"},
+          cpu_baseline=cpu, gpu_launches=E.launches)
 
 
 if __name__ == "__main__":

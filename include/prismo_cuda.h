@@ -284,6 +284,42 @@ int64_t pc_batch_launch_count(const pc_batch* b);
 int64_t pc_batch_steps_done(const pc_batch* b);
 void pc_batch_destroy(pc_batch* b);
 
+/* ------------------------------------------------------------------------- *
+ * Surrogate network.  No counterpart in the reference (it has no learned
+ * model): an ensemble of `members` MLPs dims[0] -> dims[1] -> dims[2] -> dims[3]
+ * -> dims[4] with SiLU after the three hidden layers, bf16 weights and
+ * activations on the tensor cores with float32 accumulation, float32 master
+ * parameters and Adam.  dims[0] <= 32 (padded to 32 internally); dims[1..4]
+ * multiples of 32.  Batches: 1..max_batch rows for the forward pass, multiples
+ * of 32 for training; max_batch a multiple of 32.
+ *
+ * Parameter vector of one member (P floats, pc_mlp_param_count): for layer
+ * l = 0..3 the weight [n_l][k_l] (row-major, k_0 = 32 with columns >= dims[0]
+ * zero) at w_off, then the bias [n_l] at b_off (pc_mlp_param_layout).  Host
+ * parameter and gradient arrays are [members][P].  Device inputs x are
+ * [members][batch][dims[0]] float32, targets and outputs [members][batch][dims[4]].
+ * ------------------------------------------------------------------------- */
+typedef struct pc_mlp pc_mlp;
+
+int pc_mlp_create(int32_t members, int32_t max_batch, const int32_t dims[5], pc_mlp** out);
+int64_t pc_mlp_param_count(const pc_mlp* n);
+/* out = {w_off, b_off, n, k} of layer l */
+int pc_mlp_param_layout(const pc_mlp* n, int32_t layer, int64_t out[4]);
+/* Load the float32 masters of every member (resets Adam's moments and step). */
+int pc_mlp_set_params(pc_mlp* n, const float* host);
+int pc_mlp_get_params(const pc_mlp* n, float* host);
+int pc_mlp_get_grads(const pc_mlp* n, float* host);
+int pc_mlp_forward(pc_mlp* n, const float* d_x, int32_t batch, float* d_y, void* stream);
+/* Forward + backward of the mean-squared error mean((y - t)^2) per member;
+ * gradients land in the gradient buffer, d_loss (device, nullable) gets
+ * [members] losses. */
+int pc_mlp_gradients(pc_mlp* n, const float* d_x, const float* d_t, int32_t batch, float* d_loss, void* stream);
+/* pc_mlp_gradients followed by one Adam step (bias-corrected). */
+int pc_mlp_train_step(pc_mlp* n, const float* d_x, const float* d_t, int32_t batch, float lr, float beta1,
+                      float beta2, float eps, float* d_loss, void* stream);
+int64_t pc_mlp_launch_count(const pc_mlp* n);
+void pc_mlp_destroy(pc_mlp* n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -145,6 +145,18 @@ SIGNATURES = {
     "pc_batch_launch_count": (C.c_int64, [C.c_void_p]),
     "pc_batch_steps_done": (C.c_int64, [C.c_void_p]),
     "pc_batch_destroy": (None, [C.c_void_p]),
+    "pc_mlp_create": (C.c_int, [C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_void_p)]),
+    "pc_mlp_param_count": (C.c_int64, [C.c_void_p]),
+    "pc_mlp_param_layout": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
+    "pc_mlp_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "pc_mlp_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "pc_mlp_get_grads": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "pc_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "pc_mlp_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "pc_mlp_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.c_float, C.c_float,
+                                    C.c_float, C.c_void_p, C.c_void_p]),
+    "pc_mlp_launch_count": (C.c_int64, [C.c_void_p]),
+    "pc_mlp_destroy": (None, [C.c_void_p]),
 }
 
 _lock = threading.Lock()

@@ -1,0 +1,559 @@
+// Surrogate network: an ensemble of small MLPs (in -> h -> h -> h -> out, SiLU)
+// mapping coupler geometry to S-parameter spectra, trained on the device.
+//
+// Every matrix product of the forward pass, the backward pass and the weight
+// gradient is one GEMM form, C[m][n] = sum_k A[m][k] B[n][k] with both operands
+// bf16 and K-contiguous, accumulated in float32 on the tensor cores
+// (mma.sync m16n8k16, bf16 x bf16 -> f32).  The layouts that make every product
+// K-contiguous are kept by the epilogues, which write each activation and each
+// back-propagated gradient twice (row-major and transposed):
+//   forward   z_l = a_l W_l^T + b_l          A = a_l [B][K],   B = W_l  [N][K]
+//   data grad g_{l-1} = (g_l W_l) * silu'(z) A = g_l [B][N],   B = W_l^T [K][N]
+//   weight    dW_l = g_l^T a_l               A = g_l^T [N][B], B = a_l^T [K][B]
+// Ensemble members run side by side on gridDim.z.  Parameters are float32
+// masters updated by Adam; the bf16 copies W and W^T the GEMMs read are written
+// by the same Adam kernel.
+#include <cuda_bf16.h>
+
+#include <vector>
+
+#include "pc_internal.cuh"
+
+namespace pc {
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+constexpr int GT = 64;   // CTA tile (M and N)
+constexpr int GK = 32;   // K chunk
+constexpr int GPAD = 8;  // smem row padding (bf16 elements)
+
+enum { EP_HIDDEN = 0, EP_OUT = 1, EP_BWD = 2, EP_WGRAD = 3 };
+
+struct GemmP {
+    const bf16* A;
+    int64_t lda, sA;
+    const bf16* B;
+    int64_t ldb, sB;
+    int M, N, K;
+    const float* bias;
+    int64_t sBias;
+    float* outF;  // z (hidden), y (out), dW (wgrad)
+    int64_t ldo, sO;
+    const float* zprev;  // bwd: pre-activation of the layer below
+    int64_t ldz, sZ;
+    bf16* outB;  // activation / gradient, row-major
+    int64_t ldb2, sOB;
+    bf16* outT;  // the same, transposed
+    int64_t ldt, sOT;
+};
+
+__device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z)); }
+
+__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint32_t* b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <int MODE>
+__device__ __forceinline__ void epilogue(const GemmP& p, int z, int m, int n, float acc) {
+    if (m >= p.M || n >= p.N) return;
+    if (MODE == EP_HIDDEN) {
+        const float v = acc + p.bias[z * p.sBias + n];
+        p.outF[z * p.sO + (int64_t)m * p.ldo + n] = v;
+        const bf16 a = __float2bfloat16_rn(v * sigm(v));
+        p.outB[z * p.sOB + (int64_t)m * p.ldb2 + n] = a;
+        p.outT[z * p.sOT + (int64_t)n * p.ldt + m] = a;
+    } else if (MODE == EP_OUT) {
+        p.outF[z * p.sO + (int64_t)m * p.ldo + n] = acc + p.bias[z * p.sBias + n];
+    } else if (MODE == EP_BWD) {
+        const float zz = p.zprev[z * p.sZ + (int64_t)m * p.ldz + n];
+        const float s = sigm(zz);
+        const bf16 g = __float2bfloat16_rn(acc * (s * (1.0f + zz * (1.0f - s))));
+        p.outB[z * p.sOB + (int64_t)m * p.ldb2 + n] = g;
+        p.outT[z * p.sOT + (int64_t)n * p.ldt + m] = g;
+    } else {
+        p.outF[z * p.sO + (int64_t)m * p.ldo + n] = acc;
+    }
+}
+
+// 64x64 tile per CTA, 4 warps of 32x32; K in chunks of 32 staged in shared memory.
+template <int MODE>
+__global__ void __launch_bounds__(128) mlp_gemm(GemmP p) {
+    __shared__ __align__(16) bf16 As[GT][GK + GPAD];
+    __shared__ __align__(16) bf16 Bs[GT][GK + GPAD];
+    const int z = blockIdx.z;
+    const int m0 = blockIdx.y * GT, n0 = blockIdx.x * GT;
+    const bf16* A = p.A + z * p.sA;
+    const bf16* B = p.B + z * p.sB;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    const int g = lane >> 2, t = lane & 3;
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+
+    for (int k0 = 0; k0 < p.K; k0 += GK) {
+        // 64 rows x 32 bf16 = 4 chunks of 16 bytes per row, per operand
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const int c = tid + r * 128;
+            const int row = c >> 2, col = (c & 3) * 8;
+            uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0);
+            if (m0 + row < p.M) va = *reinterpret_cast<const uint4*>(A + (int64_t)(m0 + row) * p.lda + k0 + col);
+            if (n0 + row < p.N) vb = *reinterpret_cast<const uint4*>(B + (int64_t)(n0 + row) * p.ldb + k0 + col);
+            *reinterpret_cast<uint4*>(&As[row][col]) = va;
+            *reinterpret_cast<uint4*>(&Bs[row][col]) = vb;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < GK; kk += 16) {
+            uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int r = wm + i * 16 + g;
+                af[i][0] = *reinterpret_cast<const uint32_t*>(&As[r][kk + 2 * t]);
+                af[i][1] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + 2 * t]);
+                af[i][2] = *reinterpret_cast<const uint32_t*>(&As[r][kk + 2 * t + 8]);
+                af[i][3] = *reinterpret_cast<const uint32_t*>(&As[r + 8][kk + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int c = wn + j * 8 + g;
+                bfr[j][0] = *reinterpret_cast<const uint32_t*>(&Bs[c][kk + 2 * t]);
+                bfr[j][1] = *reinterpret_cast<const uint32_t*>(&Bs[c][kk + 2 * t + 8]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int m = m0 + wm + i * 16 + g, n = n0 + wn + j * 8 + 2 * t;
+            epilogue<MODE>(p, z, m, n, acc[i][j][0]);
+            epilogue<MODE>(p, z, m, n + 1, acc[i][j][1]);
+            epilogue<MODE>(p, z, m + 8, n, acc[i][j][2]);
+            epilogue<MODE>(p, z, m + 8, n + 1, acc[i][j][3]);
+        }
+}
+
+// x [z][B][din] float -> bf16 [z][B][kp] and [z][kp][B] (member stride Bmax * kp), zero padded
+__global__ void mlp_pack(const float* __restrict__ x, int din, int kp, int B, int Bmax, bf16* __restrict__ xb,
+                         bf16* __restrict__ xt) {
+    const int z = blockIdx.y;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < B * kp; e += gridDim.x * blockDim.x) {
+        const int b = e / kp, k = e - (e / kp) * kp;
+        const float v = k < din ? x[((int64_t)z * B + b) * din + k] : 0.f;
+        const bf16 h = __float2bfloat16_rn(v);
+        xb[(int64_t)z * Bmax * kp + e] = h;
+        xt[(int64_t)z * Bmax * kp + (int64_t)k * B + b] = h;
+    }
+}
+
+// mean-squared error over [B][N]; g = 2 (y - t) / (B N) as bf16 (both layouts).
+// y, g, g^T have member stride Bmax * N; targets are dense [z][B][N].
+__global__ void mlp_mse(const float* __restrict__ y, const float* __restrict__ tg, int B, int Bmax, int N,
+                        bf16* __restrict__ g, bf16* __restrict__ gt, float* __restrict__ loss) {
+    const int z = blockIdx.y;
+    const int64_t off = (int64_t)z * Bmax * N;
+    const float sc = 2.0f / ((float)B * (float)N);
+    float acc = 0.f;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < B * N; e += gridDim.x * blockDim.x) {
+        const float d = y[off + e] - tg[(int64_t)z * B * N + e];
+        acc += d * d;
+        const int b = e / N, n = e - (e / N) * N;
+        const bf16 h = __float2bfloat16_rn(sc * d);
+        g[off + e] = h;
+        gt[off + (int64_t)n * B + b] = h;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0 && loss) atomicAdd(&loss[z], acc / ((float)B * (float)N));
+}
+
+// bias gradient: db[n] = sum_b g^T[n][b], one warp per n (member stride Bmax * N)
+__global__ void mlp_bias_grad(const bf16* __restrict__ gt, int N, int B, int Bmax, float* __restrict__ db,
+                              int64_t sDb) {
+    const int z = blockIdx.y;
+    const int n = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    if (n >= N) return;
+    const bf16* row = gt + (int64_t)z * Bmax * N + (int64_t)n * B;
+    float s = 0.f;
+    for (int b = threadIdx.x & 31; b < B; b += 32) s += __bfloat162float(row[b]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) db[z * sDb + n] = s;
+}
+
+struct LayerSeg {
+    int64_t w_off, b_off;  // into the per-member parameter vector
+    int n, k;              // weight [n][k] (k padded)
+};
+
+// Adam on the float32 masters; weight entries also refresh the bf16 W and W^T
+struct AdamP {
+    float* w;
+    const float* g;
+    float* m;
+    float* v;
+    int64_t P;
+    float lr_t, b1, b2, eps;
+    LayerSeg seg[4];
+    bf16* wb[4];
+    bf16* wt[4];
+    int64_t swb[4];
+};
+
+__global__ void mlp_adam(AdamP a) {
+    const int z = blockIdx.y;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.P; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t o = z * a.P + e;
+        const float gr = a.g[o];
+        const float m = a.b1 * a.m[o] + (1.f - a.b1) * gr;
+        const float v = a.b2 * a.v[o] + (1.f - a.b2) * gr * gr;
+        a.m[o] = m;
+        a.v[o] = v;
+        const float w = a.w[o] - a.lr_t * m / (sqrtf(v) + a.eps);
+        a.w[o] = w;
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const LayerSeg& s = a.seg[l];
+            const int64_t r = e - s.w_off;
+            if (r >= 0 && r < (int64_t)s.n * s.k) {
+                const int n = (int)(r / s.k), k = (int)(r - (r / s.k) * s.k);
+                const bf16 h = __float2bfloat16_rn(w);
+                a.wb[l][z * a.swb[l] + r] = h;
+                a.wt[l][z * a.swb[l] + (int64_t)k * s.n + n] = h;
+            }
+        }
+    }
+}
+
+// refresh the bf16 copies from the masters (after pc_mlp_set_params)
+__global__ void mlp_sync_bf16(AdamP a) {
+    const int z = blockIdx.y;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < a.P; e += (int64_t)gridDim.x * blockDim.x) {
+        const float w = a.w[z * a.P + e];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const LayerSeg& s = a.seg[l];
+            const int64_t r = e - s.w_off;
+            if (r >= 0 && r < (int64_t)s.n * s.k) {
+                const int n = (int)(r / s.k), k = (int)(r - (r / s.k) * s.k);
+                const bf16 h = __float2bfloat16_rn(w);
+                a.wb[l][z * a.swb[l] + r] = h;
+                a.wt[l][z * a.swb[l] + (int64_t)k * s.n + n] = h;
+            }
+        }
+    }
+}
+
+}  // namespace
+}  // namespace pc
+
+using namespace pc;
+
+struct pc_mlp {
+    int members = 0, max_batch = 0;
+    int din = 0;
+    int kp[4] = {}, nn[4] = {};  // per layer: padded input width, output width
+    LayerSeg seg[4] = {};
+    int64_t P = 0;
+    float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+    bf16* wb[4] = {};
+    bf16* wt[4] = {};
+    bf16 *xb = nullptr, *xt = nullptr;
+    float* z[3] = {};
+    bf16* act[3] = {};   // inputs of layers 1..3
+    bf16* actT[3] = {};
+    float* y = nullptr;
+    bf16* gr[4] = {};    // gradients w.r.t. pre-activations of layers 0..3
+    bf16* grT[4] = {};
+    float* d_loss = nullptr;
+    long long t = 0;     // Adam steps taken
+    long long launches = 0;
+    std::vector<void*> allocs;
+};
+
+namespace pc {
+namespace {
+
+template <typename T>
+int mlp_alloc(pc_mlp* n, T** p, size_t count) {
+    void* q = nullptr;
+    PC_CUDA_CHECK(cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T)));
+    PC_CUDA_CHECK(cudaMemset(q, 0, std::max<size_t>(count, 1) * sizeof(T)));
+    n->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return PC_OK;
+}
+
+AdamP adam_args(pc_mlp* n) {
+    AdamP a{};
+    a.w = n->w;
+    a.g = n->g;
+    a.m = n->m;
+    a.v = n->v;
+    a.P = n->P;
+    for (int l = 0; l < 4; ++l) {
+        a.seg[l] = n->seg[l];
+        a.wb[l] = n->wb[l];
+        a.wt[l] = n->wt[l];
+        a.swb[l] = (int64_t)n->nn[l] * n->kp[l];
+    }
+    return a;
+}
+
+template <int MODE>
+int gemm(pc_mlp* n, GemmP p, cudaStream_t s) {
+    dim3 grd((p.N + GT - 1) / GT, (p.M + GT - 1) / GT, n->members);
+    mlp_gemm<MODE><<<grd, 128, 0, s>>>(p);
+    ++n->launches;
+    PC_CUDA_CHECK(cudaGetLastError());
+    return PC_OK;
+}
+
+// forward of every member on x [members][B][din]; leaves z, activations, y
+int forward(pc_mlp* n, const float* x, int B, cudaStream_t s) {
+    const int M = n->members;
+    mlp_pack<<<dim3(std::min(1024, (B * n->kp[0] + 255) / 256), M), 256, 0, s>>>(x, n->din, n->kp[0], B, n->max_batch,
+                                                                                 n->xb, n->xt);
+    ++n->launches;
+    for (int l = 0; l < 4; ++l) {
+        GemmP p{};
+        p.A = l == 0 ? n->xb : n->act[l - 1];
+        p.lda = n->kp[l];
+        p.sA = (int64_t)n->max_batch * n->kp[l];
+        p.B = n->wb[l];
+        p.ldb = n->kp[l];
+        p.sB = (int64_t)n->nn[l] * n->kp[l];
+        p.M = B;
+        p.N = n->nn[l];
+        p.K = n->kp[l];
+        p.bias = n->w + n->seg[l].b_off;
+        p.sBias = n->P;
+        int rc;
+        if (l < 3) {
+            p.outF = n->z[l];
+            p.ldo = n->nn[l];
+            p.sO = (int64_t)n->max_batch * n->nn[l];
+            p.outB = n->act[l];
+            p.ldb2 = n->nn[l];
+            p.sOB = (int64_t)n->max_batch * n->nn[l];
+            p.outT = n->actT[l];
+            p.ldt = B;
+            p.sOT = (int64_t)n->max_batch * n->nn[l];
+            rc = gemm<EP_HIDDEN>(n, p, s);
+        } else {
+            p.outF = n->y;
+            p.ldo = n->nn[3];
+            p.sO = (int64_t)n->max_batch * n->nn[3];
+            rc = gemm<EP_OUT>(n, p, s);
+        }
+        if (rc) return rc;
+    }
+    return PC_OK;
+}
+
+// loss and gradients w.r.t. every parameter (into n->g)
+int backward(pc_mlp* n, const float* tg, int B, float* loss, cudaStream_t s) {
+    const int M = n->members;
+    const int N3 = n->nn[3];
+    mlp_mse<<<dim3(std::min(1024, (B * N3 + 255) / 256), M), 256, 0, s>>>(n->y, tg, B, n->max_batch, N3, n->gr[3],
+                                                                          n->grT[3], loss);
+    ++n->launches;
+    for (int l = 3; l >= 0; --l) {
+        // weight gradient: dW[n][k] = sum_b g^T[n][b] a^T[k][b]
+        GemmP p{};
+        p.A = n->grT[l];
+        p.lda = B;
+        p.sA = (int64_t)n->max_batch * n->nn[l];
+        p.B = l == 0 ? n->xt : n->actT[l - 1];
+        p.ldb = B;
+        p.sB = (int64_t)n->max_batch * n->kp[l];
+        p.M = n->nn[l];
+        p.N = n->kp[l];
+        p.K = B;
+        p.outF = n->g + n->seg[l].w_off;
+        p.ldo = n->kp[l];
+        p.sO = n->P;
+        int rc = gemm<EP_WGRAD>(n, p, s);
+        if (rc) return rc;
+        mlp_bias_grad<<<dim3((n->nn[l] + 7) / 8, M), 256, 0, s>>>(n->grT[l], n->nn[l], B, n->max_batch,
+                                                                   n->g + n->seg[l].b_off, n->P);
+        ++n->launches;
+        if (l == 0) break;
+        // data gradient into the layer below: g_{l-1} = (g_l W_l) * silu'(z_{l-1})
+        GemmP q{};
+        q.A = n->gr[l];
+        q.lda = n->nn[l];
+        q.sA = (int64_t)n->max_batch * n->nn[l];
+        q.B = n->wt[l];
+        q.ldb = n->nn[l];
+        q.sB = (int64_t)n->nn[l] * n->kp[l];
+        q.M = B;
+        q.N = n->kp[l];
+        q.K = n->nn[l];
+        q.zprev = n->z[l - 1];
+        q.ldz = n->nn[l - 1];
+        q.sZ = (int64_t)n->max_batch * n->nn[l - 1];
+        q.outB = n->gr[l - 1];
+        q.ldb2 = n->nn[l - 1];
+        q.sOB = (int64_t)n->max_batch * n->nn[l - 1];
+        q.outT = n->grT[l - 1];
+        q.ldt = B;
+        q.sOT = (int64_t)n->max_batch * n->nn[l - 1];
+        rc = gemm<EP_BWD>(n, q, s);
+        if (rc) return rc;
+    }
+    return PC_OK;
+}
+
+}  // namespace
+}  // namespace pc
+
+extern "C" {
+
+int pc_mlp_create(int32_t members, int32_t max_batch, const int32_t dims[5], pc_mlp** out) {
+    if (!out || !dims || members <= 0 || members > 64 || max_batch <= 0 || max_batch % 32 != 0 ||
+        max_batch > (1 << 20))
+        return PC_ERR_INVALID;
+    if (dims[0] <= 0 || dims[0] > 32) return PC_ERR_INVALID;
+    for (int l = 1; l < 5; ++l)
+        if (dims[l] <= 0 || dims[l] % 32 != 0 || dims[l] > 4096) return PC_ERR_INVALID;
+    *out = nullptr;
+    pc_mlp* n = new pc_mlp();
+    n->members = members;
+    n->max_batch = max_batch;
+    n->din = dims[0];
+    int64_t off = 0;
+    for (int l = 0; l < 4; ++l) {
+        n->kp[l] = l == 0 ? 32 : dims[l];
+        n->nn[l] = dims[l + 1];
+        n->seg[l].n = n->nn[l];
+        n->seg[l].k = n->kp[l];
+        n->seg[l].w_off = off;
+        off += (int64_t)n->nn[l] * n->kp[l];
+        n->seg[l].b_off = off;
+        off += n->nn[l];
+    }
+    n->P = off;
+    const size_t Mb = (size_t)members, B = (size_t)max_batch;
+    int rc = mlp_alloc(n, &n->w, Mb * off) || mlp_alloc(n, &n->g, Mb * off) || mlp_alloc(n, &n->m, Mb * off) ||
+             mlp_alloc(n, &n->v, Mb * off) || mlp_alloc(n, &n->xb, Mb * B * 32) || mlp_alloc(n, &n->xt, Mb * B * 32) ||
+             mlp_alloc(n, &n->y, Mb * B * n->nn[3]) || mlp_alloc(n, &n->d_loss, Mb);
+    for (int l = 0; l < 4 && !rc; ++l) {
+        rc = mlp_alloc(n, &n->wb[l], Mb * n->nn[l] * n->kp[l]) || mlp_alloc(n, &n->wt[l], Mb * n->nn[l] * n->kp[l]) ||
+             mlp_alloc(n, &n->gr[l], Mb * B * n->nn[l]) || mlp_alloc(n, &n->grT[l], Mb * B * n->nn[l]);
+        if (!rc && l < 3)
+            rc = mlp_alloc(n, &n->z[l], Mb * B * n->nn[l]) || mlp_alloc(n, &n->act[l], Mb * B * n->nn[l]) ||
+                 mlp_alloc(n, &n->actT[l], Mb * B * n->nn[l]);
+    }
+    if (rc) {
+        pc_mlp_destroy(n);
+        return PC_ERR_CUDA;
+    }
+    *out = n;
+    return PC_OK;
+}
+
+int64_t pc_mlp_param_count(const pc_mlp* n) { return n ? n->P : PC_ERR_INVALID; }
+
+int pc_mlp_param_layout(const pc_mlp* n, int32_t layer, int64_t out[4]) {
+    if (!n || !out || layer < 0 || layer > 3) return PC_ERR_INVALID;
+    out[0] = n->seg[layer].w_off;
+    out[1] = n->seg[layer].b_off;
+    out[2] = n->seg[layer].n;
+    out[3] = n->seg[layer].k;
+    return PC_OK;
+}
+
+int pc_mlp_set_params(pc_mlp* n, const float* host) {
+    if (!n || !host) return PC_ERR_INVALID;
+    const size_t bytes = (size_t)n->members * n->P * sizeof(float);
+    PC_CUDA_CHECK(cudaMemcpy(n->w, host, bytes, cudaMemcpyHostToDevice));
+    PC_CUDA_CHECK(cudaMemset(n->m, 0, bytes));
+    PC_CUDA_CHECK(cudaMemset(n->v, 0, bytes));
+    n->t = 0;
+    AdamP a = adam_args(n);
+    mlp_sync_bf16<<<dim3(std::min<int64_t>(1024, (n->P + 255) / 256), n->members), 256>>>(a);
+    ++n->launches;
+    PC_CUDA_CHECK(cudaGetLastError());
+    PC_CUDA_CHECK(cudaDeviceSynchronize());
+    return PC_OK;
+}
+
+int pc_mlp_get_params(const pc_mlp* n, float* host) {
+    if (!n || !host) return PC_ERR_INVALID;
+    PC_CUDA_CHECK(cudaMemcpy(host, n->w, (size_t)n->members * n->P * sizeof(float), cudaMemcpyDeviceToHost));
+    return PC_OK;
+}
+
+int pc_mlp_get_grads(const pc_mlp* n, float* host) {
+    if (!n || !host) return PC_ERR_INVALID;
+    PC_CUDA_CHECK(cudaMemcpy(host, n->g, (size_t)n->members * n->P * sizeof(float), cudaMemcpyDeviceToHost));
+    return PC_OK;
+}
+
+int pc_mlp_forward(pc_mlp* n, const float* d_x, int32_t batch, float* d_y, void* stream) {
+    if (!n || !d_x || !d_y || batch <= 0 || batch > n->max_batch) return PC_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = forward(n, d_x, batch, s);
+    if (rc) return rc;
+    const size_t row = (size_t)n->nn[3] * sizeof(float);
+    PC_CUDA_CHECK(cudaMemcpy2DAsync(d_y, (size_t)batch * row, n->y, (size_t)n->max_batch * row, (size_t)batch * row,
+                                    n->members, cudaMemcpyDeviceToDevice, s));
+    return PC_OK;
+}
+
+int pc_mlp_gradients(pc_mlp* n, const float* d_x, const float* d_t, int32_t batch, float* d_loss, void* stream) {
+    if (!n || !d_x || !d_t || batch <= 0 || batch > n->max_batch || batch % 32 != 0) return PC_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    PC_CUDA_CHECK(cudaMemsetAsync(n->d_loss, 0, n->members * sizeof(float), s));
+    int rc = forward(n, d_x, batch, s);
+    if (rc) return rc;
+    rc = backward(n, d_t, batch, n->d_loss, s);
+    if (rc) return rc;
+    if (d_loss)
+        PC_CUDA_CHECK(
+            cudaMemcpyAsync(d_loss, n->d_loss, n->members * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    return PC_OK;
+}
+
+int pc_mlp_train_step(pc_mlp* n, const float* d_x, const float* d_t, int32_t batch, float lr, float beta1,
+                      float beta2, float eps, float* d_loss, void* stream) {
+    if (!n || !(lr > 0) || !(beta1 >= 0 && beta1 < 1) || !(beta2 >= 0 && beta2 < 1) || !(eps > 0))
+        return PC_ERR_INVALID;
+    int rc = pc_mlp_gradients(n, d_x, d_t, batch, d_loss, stream);
+    if (rc) return rc;
+    ++n->t;
+    AdamP a = adam_args(n);
+    a.b1 = beta1;
+    a.b2 = beta2;
+    a.eps = eps;
+    a.lr_t = (float)(lr * sqrt(1.0 - pow((double)beta2, (double)n->t)) / (1.0 - pow((double)beta1, (double)n->t)));
+    mlp_adam<<<dim3(std::min<int64_t>(1024, (n->P + 255) / 256), n->members), 256, 0, (cudaStream_t)stream>>>(a);
+    ++n->launches;
+    PC_CUDA_CHECK(cudaGetLastError());
+    return PC_OK;
+}
+
+int64_t pc_mlp_launch_count(const pc_mlp* n) { return n ? n->launches : PC_ERR_INVALID; }
+
+void pc_mlp_destroy(pc_mlp* n) {
+    if (!n) return;
+    for (void* p : n->allocs) cudaFree(p);
+    delete n;
+}
+
+}  // extern "C"

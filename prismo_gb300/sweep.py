@@ -491,6 +491,7 @@ class SweepResult:
     cell_steps: int
     launches: int = 0
     variant: int = -1
+    run_seconds: float = 0.0
 
     @property
     def designs_per_s(self) -> float:
@@ -499,22 +500,31 @@ class SweepResult:
 
 def batched_sweep(designs: Sequence[CouplerDesign], nsteps: int = STEPS, nfreq: int = NFREQ, device=None,
                   autotune: bool = True, layouts=None, variant: Optional[int] = None) -> SweepResult:
-    """S-parameters of every design from one batched run (couplers + normalisations)."""
+    """S-parameters of every design from one batched run (couplers + normalisations).
+
+    ``seconds`` runs from the design list to the S-parameters (layouts, device
+    setup, time loop, spectra); ``run_seconds`` is the time loop and spectra."""
     import torch
 
+    dev = torch.device(device or "cuda")
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
     layouts = layouts or [coupler_layout(d) for d in designs]
     freqs = sweep_freqs(nfreq)
-    B = BatchedFDTD2D(instances_for(layouts), freqs, device=device, autotune=autotune, variant=variant)
+    B = BatchedFDTD2D(instances_for(layouts), freqs, device=dev, autotune=autotune, variant=variant)
     try:
         torch.cuda.synchronize(B.device)
         l0 = B.launches
-        t0 = time.perf_counter()
+        t1 = time.perf_counter()
         B.run(nsteps)
         spec = B.spectra()
-        dt_s = time.perf_counter() - t0
+        t2 = time.perf_counter()
         S = np.stack([s_parameters(spec[2 * q], spec[2 * q + 1][0], L) for q, L in enumerate(layouts)])
+        t3 = time.perf_counter()
         cells = sum(I.eps.shape[0] * I.eps.shape[1] for I in B.instances) * nsteps
-        return SweepResult(list(designs), list(layouts), S, dt_s, cells, B.launches - l0, B.tuning()[0])
+        r = SweepResult(list(designs), list(layouts), S, t3 - t0, cells, B.launches - l0, B.tuning()[0])
+        r.run_seconds = t2 - t1
+        return r
     finally:
         B.close()
 
@@ -522,21 +532,22 @@ def batched_sweep(designs: Sequence[CouplerDesign], nsteps: int = STEPS, nfreq: 
 def serial_sweep(designs: Sequence[CouplerDesign], nsteps: int = STEPS, nfreq: int = NFREQ, device=None,
                  layouts=None) -> SweepResult:
     """The plain path: one single-simulation 2D engine per coupler and per
-    normalisation run, one after another (ParameterSweep's sequential loop)."""
+    normalisation run, one after another (ParameterSweep's sequential loop).
+    Timed like ``batched_sweep``: from the design list to the S-parameters."""
     import torch
 
     from .engine import FDTDEngine
 
+    dev = torch.device(device or "cuda")
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
     layouts = layouts or [coupler_layout(d) for d in designs]
     freqs = sweep_freqs(nfreq)
     dt = sweep_dt()
     amps = amplitudes(nsteps, dt)[:, None]
-    dev = torch.device(device or "cuda")
     S = []
     cells = 0
     launches = 0
-    torch.cuda.synchronize(dev)
-    t0 = time.perf_counter()
     for L in layouts:
         spec = []
         for eps, ports in ((L.eps, L.ports), (L.norm_eps, L.ports[:1])):

@@ -143,3 +143,67 @@ def config_3d_dispersive(dims=(384, 384, 192), seed=0, dx=20e-9, z_metal=None):
     box = (0, nx, 0, ny, 0, zm)
     k_plane = min(nz - 12 - 8, zm + ridge_h + (nz - zm - ridge_h) // 2)
     return eps, box, lor, k_plane
+
+
+def dispersive_monitor_planes(dims, z_metal, ridge_h, k_plane):
+    """Ex DFT planes (Ex indices, all x and y): halfway between the ridge top and
+    the TFSF plane, and 2 cells inside the metal."""
+    nx, ny, nz = dims
+    k_up = (z_metal + ridge_h + k_plane) // 2
+    k_dn = max(1, z_metal - 2)
+    idx = lambda k: (np.arange(nx)[:, None, None], np.arange(ny - 1)[None, :, None], np.array([[[k]]]))  # noqa: E731
+    return [idx(k_up), idx(k_dn)]
+
+
+def build_dispersive_engine(dims=(384, 384, 192), precision="fp32", cpml=12, dx=20e-9, nfreq=64, seed=0,
+                            z_metal=None, ridge_width=1.0e-6, device="cuda:0"):
+    """The 3D dispersive configuration on the device engine: Drude + 2 Lorentz
+    half-space metal (eps_inf 1) under a Si3N4 ridge, Ex-polarised plane wave
+    injected by a TFSF plane above the ridge travelling towards the metal (-z),
+    and two 64-frequency Ex DFT planes (1.5-1.6 um).  Returns (engine, info)
+    with info holding dt, eps, the metal box, the pole dicts, the TFSF plane,
+    the waveform and the monitor index sets."""
+    from .engine import FDTDEngine
+    from .materials import DrudeLorentzMaterial
+    from .pml import PMLParams
+    from .sources import GaussianPulse
+
+    nx, ny, nz = dims
+    zm = z_metal if z_metal is not None else nz // 2
+    eps, box, lor, k_plane = config_3d_dispersive(dims, seed=seed, dx=dx, z_metal=zm)
+    if ridge_width != 1.0e-6:  # reduced grids: narrower ridge
+        eps = np.ones(dims)
+        ridge_h = int(round(0.4e-6 / dx))
+        my = _axis_mask(ny, ny / 2.0, ridge_width / dx)
+        eps[:, my, zm:zm + ridge_h] = 4.0
+    ridge_h = int(round(0.4e-6 / dx))
+    k_plane = min(nz - cpml - 8, zm + ridge_h + (nz - zm - ridge_h) // 2)
+    dt = 0.5 / (C0 * np.sqrt(3.0 / dx**2))
+    metal = DrudeLorentzMaterial(1.0, 1.37e16, 1.0e14, lor)
+    poles = metal.ade_poles(dt)
+    wf = GaussianPulse(193e12, 10e-15)
+    eng = FDTDEngine(dims, (dx, dx, dx), dt, is_2d=False, precision=precision, material_arrays={"eps_rel": eps},
+                     pml=PMLParams(thickness=cpml), device=device)
+    eng.set_dispersive([(box, 1.0, poles)])
+    eng.set_tfsf(k_plane, -1, "x", wf)
+    planes = dispersive_monitor_planes(dims, zm, ridge_h, k_plane)
+    freqs = wavelengths_to_freqs(1.5e-6, 1.6e-6, nfreq)
+    mids = [eng.add_dft("Ex", eng.offsets("Ex", p), freqs, t0=dt) for p in planes]
+    info = dict(dt=dt, eps=eps, box=box, poles=poles, k_plane=k_plane, waveform=wf, planes=planes, freqs=freqs,
+                dft_ids=mids, z_metal=zm, ridge_h=ridge_h)
+    return eng, info
+
+
+def dispersive_bytes_per_cell(dims, cpml, box, npoles_lorentz, nplanes, nfreq):
+    """Algorithmic float32 bytes per cell update of the dispersive configuration:
+    6 fields R+W and 3 Cb (60 B), CPML psi on the slabs (32 B x slab fraction per
+    axis), the ADE auxiliaries on metal cells (Drude J: 3 x 8 B; each Lorentz
+    pole P and P_prev: 3 x 12 B) and the DFT accumulators on the monitor planes
+    (16 B R+W per frequency per plane point, sampled Ex)."""
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    b = 60.0 + 32.0 * sum(2.0 * cpml / m for m in dims)
+    metal = (box[1] - box[0]) * (box[3] - box[2]) * (box[5] - box[4]) / n
+    b += metal * (3 * 8 + npoles_lorentz * 3 * 12)
+    b += nplanes * nx * ny / n * nfreq * 32 / 16.0  # accumulators touched once per 16 steps
+    return b

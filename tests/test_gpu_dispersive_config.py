@@ -1,0 +1,57 @@
+"""The 3D dispersive configuration (Drude + 2 Lorentz metal half-space, Si3N4
+ridge, TFSF plane wave, two 64-frequency Ex DFT planes) at reduced size against
+the float64 oracle: float32 fields rel L2 <= 1e-5, DFT planes <= 1e-4 per
+frequency; float64 fields |err| <= 1e-11 x max."""
+
+import numpy as np
+import pytest
+
+from oracle import fdtd64 as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_dispersive_config_reduced(torch):
+    from prismo_gb300.workloads import build_dispersive_engine
+
+    dims, cpml, n = (40, 36, 64), 6, 700
+    results = {}
+    for prec in ("fp64", "fp32"):
+        eng, info = build_dispersive_engine(dims, precision=prec, cpml=cpml, z_metal=24, ridge_width=0.3e-6)
+        dt, wf = info["dt"], info["waveform"]
+        t = (np.arange(n) + 1) * dt
+        eng.step(n, wf(t)[:, None])
+        assert eng.check_status() == 0
+        results[prec] = ({c: eng.component(c).double().cpu().numpy() for c in O.COMPONENTS},
+                         [eng.dft_result(m).cpu().numpy() for m in info["dft_ids"]])
+        eng.close()
+    g = O.OracleGrid.from_total(*dims, 20e-9, cpml)
+    o = O.OracleFDTD(g, info["dt"], {"eps_rel": info["eps"]}, cpml_layers=cpml,
+                     ade=[O.ADERegion(box=info["box"], eps_inf=1.0, poles=info["poles"])],
+                     tfsf=O.TFSFPlane(k0=info["k_plane"], direction=-1, polarization="x", waveform=info["waveform"]))
+    ids = [o.add_dft("Ex", p, info["freqs"]) for p in info["planes"]]
+    o.run(n)
+    assert np.abs(o.F["Ex"][:, :, : info["z_metal"]]).max() > 0  # the wave reached the metal
+    f64, d64 = results["fp64"]
+    f32, d32 = results["fp32"]
+    for c in O.COMPONENTS:
+        ref = o.F[c]
+        np.testing.assert_allclose(f64[c], ref, rtol=0, atol=1e-11 * np.abs(ref).max(), err_msg=c)
+        assert rel(f32[c], ref) <= 1e-5, (c, rel(f32[c], ref))
+    for q, m in enumerate(ids):
+        want = o.dfts[m].data.reshape(len(info["freqs"]), -1)
+        for f in range(want.shape[0]):
+            assert rel(d32[q][f], want[f]) <= 1e-4, (q, f, rel(d32[q][f], want[f]))

@@ -1,0 +1,113 @@
+"""Surrogate kernels (pc_mlp_*) against the float64 oracle (oracle/mlp64.py).
+
+The device computes with bf16 operands and float32 accumulation, so it is
+compared with the oracle evaluated on the same bf16-rounded parameters and
+inputs; the remaining differences come from bf16 rounding of activations and
+back-propagated gradients (about 2^-9 relative each):
+  forward output rel L2 <= 1e-2, per-layer gradient rel L2 <= 3e-2,
+  one Adam step: |w_dev - w_oracle(g_dev)| <= 1e-6 + 1e-5 |w|.
+Members are independent (each one checked against its own oracle).
+"""
+
+import numpy as np
+import pytest
+
+from oracle import mlp64
+
+pytestmark = pytest.mark.gpu
+
+DIMS = (3, 256, 256, 256, 512)
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def bf16_round(a):
+    import torch
+
+    return torch.tensor(np.asarray(a, dtype=np.float32)).to(torch.bfloat16).to(torch.float32).numpy().astype(np.float64)
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def make(torch, members=2, batch=64, seed=0):
+    from prismo_gb300.surrogate import Ensemble
+
+    E = Ensemble(members=members, dims=DIMS, max_batch=batch, seed=seed)
+    rng = np.random.default_rng(seed)
+    p = E.params().astype(np.float64)
+    segs, _ = mlp64.layout(DIMS)
+    for m in range(members):
+        for w_off, b_off, n, k in segs:
+            p[m, b_off:b_off + n] = 0.05 * rng.standard_normal(n)
+    p = bf16_round(p)  # the device's bf16 weight copies then equal the masters
+    E.set_params(p)
+    x = bf16_round(rng.uniform(-1, 1, size=(members, batch, 3)))
+    t = rng.standard_normal((members, batch, DIMS[-1]))
+    return E, p, x, t
+
+
+def test_forward_matches_oracle(torch):
+    E, p, x, t = make(torch)
+    y = E.forward_raw(torch.tensor(x, dtype=torch.float32, device="cuda")).cpu().numpy()
+    for m in range(E.members):
+        want, _ = mlp64.forward(p[m], x[m], DIMS)
+        assert rel(y[m], want) <= 1e-2, rel(y[m], want)
+    # a partial batch (rows < max_batch) gives the same rows
+    y2 = E.forward_raw(torch.tensor(x[:, :20], dtype=torch.float32, device="cuda")).cpu().numpy()
+    np.testing.assert_array_equal(y2, y[:, :20])
+    E.close()
+
+
+def test_gradients_match_oracle(torch):
+    E, p, x, t = make(torch, seed=3)
+    loss = E.gradients_raw(torch.tensor(x, dtype=torch.float32, device="cuda"),
+                           torch.tensor(t, dtype=torch.float32, device="cuda")).cpu().numpy()
+    g = E.grads()
+    segs, _ = mlp64.layout(DIMS)
+    for m in range(E.members):
+        l_o, g_o = mlp64.loss_and_grads(p[m], x[m], t[m], DIMS)
+        assert abs(loss[m] - l_o) <= 1e-3 * l_o, (loss[m], l_o)
+        for l, (w_off, b_off, n, k) in enumerate(segs):
+            gw, gw_o = g[m, w_off:w_off + n * k], g_o[w_off:w_off + n * k]
+            gb, gb_o = g[m, b_off:b_off + n], g_o[b_off:b_off + n]
+            assert rel(gw, gw_o) <= 3e-2, (m, l, "W", rel(gw, gw_o))
+            assert rel(gb, gb_o) <= 3e-2, (m, l, "b", rel(gb, gb_o))
+        w_off, _, n, k = segs[0]
+        assert np.all(g[m, w_off:w_off + n * k].reshape(n, k)[:, 3:] == 0)
+    E.close()
+
+
+def test_adam_step_and_training_progress(torch):
+    E, p, x, t = make(torch, seed=5)
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda")
+    td = torch.tensor(t, dtype=torch.float32, device="cuda")
+    E.gradients_raw(xd, td)
+    g = E.grads().astype(np.float64)
+    E.set_params(p)  # reset Adam
+    E.train_step_raw(xd, td, 1e-3)
+    got = E.params()
+    for m in range(E.members):
+        want, _, _ = mlp64.adam_step(p[m], g[m], np.zeros_like(p[m]), np.zeros_like(p[m]), 1, 1e-3)
+        np.testing.assert_allclose(got[m], want, rtol=1e-5, atol=1e-6)
+    # fit a smooth target: the loss falls by 10x in 300 steps on every member
+    rng = np.random.default_rng(7)
+    xs = rng.uniform(-1, 1, size=(E.members, 64, 3))
+    w = rng.standard_normal((3, DIMS[-1]))
+    ts = np.sin(xs @ w)
+    xd = torch.tensor(xs, dtype=torch.float32, device="cuda")
+    td = torch.tensor(ts, dtype=torch.float32, device="cuda")
+    first = E.gradients_raw(xd, td).cpu().numpy().copy()
+    for _ in range(300):
+        last = E.train_step_raw(xd, td, 2e-3)
+    last = E.gradients_raw(xd, td).cpu().numpy()
+    assert np.all(last < 0.1 * first), (first, last)
+    E.close()
