@@ -236,8 +236,23 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
     };
     auto og = [&](int pl, int r) { return (int64_t)pl * PR + (int64_t)pj[r] * P + pk[r]; };
     // CTA-uniform: does the tile touch a y or z slab (then every plane needs CPML)?
-    const bool yz_slab = CPML && (j0 < t || j0 + TY > ny - t || k0 < t || k0 + TZ > nz - t);
+    // (the +1 halo row/column of H counts: E at the tile edge reads it)
+    const bool yz_slab = CPML && (j0 < t || j0 + TY >= ny - t || k0 < t || k0 + TZ >= nz - t);
     auto x_slab = [&](int pl) { return CPML && pl >= 0 && pl < nx && (pl < t || pl >= nx - t); };
+    // L2 prefetch of the Cb values plane pl's E update will read: their loads are
+    // issued only one phase ahead of their use.  Variant without CPML code only:
+    // in the CPML variant the extra addressing spills registers, and prefetching
+    // the psi entries the same way measured slower.
+    auto prefetch_plane = [&](int pl) {
+        if (CPML || helper || pl < ib || pl >= ie) return;  // (the CPML variant has no registers to spare)
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            if (!pin[r]) continue;
+            const int64_t o = og(pl, r);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) prefetch_l2(a.cb[c] + o);
+        }
+    };
 
     // ---- H^{n+1/2} at one point --------------------------------------------
     auto h_compute = [&](const T* E0, const T* E1, const T* E2, const T* Ep1, const T* Ep2, const T* H0,
@@ -302,9 +317,12 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
         for (int r = 0; r < 2; ++r) fetch(pt_at(ib, r), true, pfH[r]);
     }
     T chk = T(0);  // running sum of E^{n+1}: non-finite iff some value was
+    constexpr int PF_AHEAD = 4;
+    for (int pl = ib; pl < ib + PF_AHEAD; ++pl) prefetch_plane(pl);
     for (; n < L; ++n) {
         const int p = ib - 1 + n;  // plane whose H^{n+1/2} is computed now
         const int q = p - 1;       // plane whose E^{n+1} is computed now
+        prefetch_plane(p + PF_AHEAD);
         const bool slabH = yz_slab || x_slab(p);
         const bool slabE = yz_slab || x_slab(q);
         const unsigned char* stc = stages + sn * G::STAGE;
@@ -487,8 +505,10 @@ struct FusedState {
     const void* key_f[2][6];
     FusedMaps maps[2];  // per input set
     bool ready = false;
-    int4* d_items = nullptr;  // work items of the current chunking
-    int n_items = 0, items_cx = -1, items_t = -1;
+    int4* d_items = nullptr;  // work items of the current chunking: plain ones, then cpml ones
+    int n_items = 0, n_plain = 0, items_cx = -1, items_t = -1;
+    cudaStream_t side = nullptr;  // the cpml class runs here, concurrently with the plain class
+    cudaEvent_t fork = nullptr, join = nullptr;
 };
 
 // One cached set of maps per context (keyed by the buffer pointers).
@@ -497,81 +517,92 @@ FusedState* state_of(pc_ctx* c) {
     return static_cast<FusedState*>(c->fused_state);
 }
 
-// Work items (k0, j0, ib, ie) for a chunk length cx, most expensive first: tiles
-// that touch a y/z CPML slab run the psi path on every plane, the others only on
-// x-slab planes (longest-processing-time-first ordering against the tail).
-static std::vector<int4> fused_items(const pc_grid_desc& g, int TY, int TZ, int cx, int t) {
-    std::vector<std::pair<double, int4>> v;
-    for (int ib = 0; ib < g.nx; ib += cx) {
-        const int ie = std::min(g.nx, ib + cx);
-        int xs = 0;
-        for (int p = ib; p < ie; ++p) xs += (t > 0 && (p < t || p >= g.nx - t)) ? 1 : 0;
+// Work items (k0, j0, ib, ie) for a chunk length cx, most expensive first
+// (longest-processing-time-first ordering against the tail).  With a CPML the
+// items fall in two classes that run as separate launches:
+//   plain: the tile and its +1 halo row/column lie outside every y/z slab and the
+//          planes [ib, ie] (ie = halo plane) outside the x slabs -> the kernel
+//          variant without CPML code;
+//   cpml:  everything else (x-chunks [0, t) and [nx-t-1, nx) of every tile, and
+//          every chunk of tiles that touch a y or z slab).
+static void fused_items(const pc_grid_desc& g, int TY, int TZ, int cx, int t, std::vector<int4>& plain,
+                        std::vector<int4>& cpml) {
+    std::vector<std::pair<int, int>> chunks;
+    if (t > 0 && g.nx > 2 * t + 2) {
+        chunks.push_back({0, t});
+        for (int ib = t; ib < g.nx - t - 1; ib += cx) chunks.push_back({ib, std::min(g.nx - t - 1, ib + cx)});
+        chunks.push_back({g.nx - t - 1, g.nx});
+    } else {
+        for (int ib = 0; ib < g.nx; ib += cx) chunks.push_back({ib, std::min(g.nx, ib + cx)});
+    }
+    std::vector<std::pair<double, int4>> vp, vc;
+    for (auto& ch : chunks) {
+        const int ib = ch.first, ie = ch.second;
+        const bool xs = t > 0 && (ib < t || ie >= g.nx - t);
         for (int j0 = 0; j0 < g.ny; j0 += TY)
             for (int k0 = 0; k0 < g.nz; k0 += TZ) {
-                const bool yz = t > 0 && (j0 < t || j0 + TY > g.ny - t || k0 < t || k0 + TZ > g.nz - t);
-                const int planes = ie - ib + 2;
-                const double cost = yz ? 3.0 * planes : (planes + 2.0 * xs);
-                v.push_back({cost, make_int4(k0, j0, ib, ie)});
+                const bool yz = t > 0 && (j0 < t || j0 + TY >= g.ny - t || k0 < t || k0 + TZ >= g.nz - t);
+                const double planes = ie - ib + 2;
+                const int4 it = make_int4(k0, j0, ib, ie);
+                if (t > 0 && (yz || xs))
+                    vc.push_back({yz ? 3.0 * planes : 2.5 * planes, it});
+                else
+                    vp.push_back({planes, it});
             }
     }
-    std::stable_sort(v.begin(), v.end(), [](const std::pair<double, int4>& x, const std::pair<double, int4>& y) {
+    auto by_cost = [](const std::pair<double, int4>& x, const std::pair<double, int4>& y) {
         return x.first > y.first;
-    });
-    std::vector<int4> out;
-    out.reserve(v.size());
-    for (auto& e : v) out.push_back(e.second);
-    return out;
+    };
+    std::stable_sort(vp.begin(), vp.end(), by_cost);
+    std::stable_sort(vc.begin(), vc.end(), by_cost);
+    plain.clear();
+    cpml.clear();
+    for (auto& e : vp) plain.push_back(e.second);
+    for (auto& e : vc) cpml.push_back(e.second);
 }
 
 template <typename T, int TY, int TZ, int S, bool CPML, bool HCOEF, bool CA>
-int launch_variant(pc_ctx* c, cudaStream_t s, const FieldArgs<T>& a, const CpmlArgs<T>& p, const FusedMaps& maps,
-                   int smem, FusedState* st) {
-    const pc_grid_desc& g = c->g;
+int launch_variant(cudaStream_t s, const FieldArgs<T>& a, const CpmlArgs<T>& p, const FusedMaps& maps, int smem,
+                   const int4* items, int n_items) {
     auto kern = fused3<T, TY, TZ, S, CPML, HCOEF, CA>;
     static bool attr = false;
     if (!attr) {
         PC_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         attr = true;
     }
-    constexpr int threads = TZ * (TY / 2 + 1);
-    int cx = c->fused_cx;
-    if (cx <= 0) {
-        int sms = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
-        if (sms <= 0) sms = 152;
-        int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
-        if (per_sm <= 0) per_sm = 1;
-        const int resident = sms * per_sm;
-        const int tiles = ((g.nz + TZ - 1) / TZ) * ((g.ny + TY - 1) / TY);
-        // enough items for ~8 per resident slot, with at most ~12% pipeline overhead
-        cx = g.nx;
-        const int cands[] = {16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512};
-        for (int cand : cands) {
-            if (cand >= g.nx) break;
-            const double items = (double)tiles * ((g.nx + cand - 1) / cand);
-            if (items >= 8.0 * resident) cx = cand;
-        }
-        if (cx == g.nx) {
-            for (int cand : cands)
-                if (cand < g.nx && (double)tiles * ((g.nx + cand - 1) / cand) >= 2.0 * resident) cx = cand;
-        }
-        c->fused_cx = cx;
-    }
-    if (st->items_cx != cx || st->items_t != p.t || !st->d_items) {
-        std::vector<int4> items = fused_items(g, TY, TZ, cx, p.t);
-        cudaFree(st->d_items);
-        st->d_items = nullptr;
-        PC_CUDA_CHECK(cudaMalloc(&st->d_items, items.size() * sizeof(int4)));
-        PC_CUDA_CHECK(cudaMemcpy(st->d_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
-        st->n_items = (int)items.size();
-        st->items_cx = cx;
-        st->items_t = p.t;
-    }
+    if (n_items <= 0) return PC_OK;
     dim3 blk(TZ, TY / 2 + 1);
-    kern<<<st->n_items, blk, smem, s>>>(a, p, st->d_items, maps);
+    kern<<<n_items, blk, smem, s>>>(a, p, items, maps);
     PC_CUDA_CHECK(cudaGetLastError());
     return PC_OK;
+}
+
+// chunk length along x: enough work items for ~8 per resident CTA slot
+template <typename T, int TY, int TZ, int S>
+int choose_chunk(const pc_grid_desc& g, int smem) {
+    auto kern = fused3<T, TY, TZ, S, true, false, false>;
+    constexpr int threads = TZ * (TY / 2 + 1);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    if (sms <= 0) sms = 152;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    if (per_sm <= 0) per_sm = 1;
+    const int resident = sms * per_sm;
+    const int tiles = ((g.nz + TZ - 1) / TZ) * ((g.ny + TY - 1) / TY);
+    int cx = g.nx;
+    const int cands[] = {16, 24, 32, 48, 64, 96, 128, 192, 256, 384, 512};
+    for (int cand : cands) {
+        if (cand >= g.nx) break;
+        const double items = (double)tiles * ((g.nx + cand - 1) / cand);
+        if (items >= 8.0 * resident) cx = cand;
+    }
+    if (cx == g.nx) {
+        for (int cand : cands)
+            if (cand < g.nx && (double)tiles * ((g.nx + cand - 1) / cand) >= 2.0 * resident) cx = cand;
+    }
+    return cx;
 }
 
 template <typename T, int TY, int TZ, int S>
@@ -601,19 +632,59 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
     const int smem = fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * PC_MAX_CPML * (int)sizeof(T);
     const bool cp = p.t > 0, hc = a.da[0] != nullptr, ca = a.ca[0] != nullptr;
     const FusedMaps& m = st->maps[in];
+    if (c->fused_cx <= 0) c->fused_cx = choose_chunk<T, TY, TZ, S>(g, smem);
+    const int cx = c->fused_cx;
+    if (st->items_cx != cx || st->items_t != p.t || !st->d_items) {
+        std::vector<int4> plain, cpml;
+        fused_items(g, TY, TZ, cx, p.t, plain, cpml);
+        plain.insert(plain.end(), cpml.begin(), cpml.end());
+        cudaFree(st->d_items);
+        st->d_items = nullptr;
+        PC_CUDA_CHECK(cudaMalloc(&st->d_items, plain.size() * sizeof(int4)));
+        PC_CUDA_CHECK(cudaMemcpy(st->d_items, plain.data(), plain.size() * sizeof(int4), cudaMemcpyHostToDevice));
+        st->n_items = (int)plain.size();
+        st->n_plain = (int)(plain.size() - cpml.size());
+        st->items_cx = cx;
+        st->items_t = p.t;
+    }
+    const int4* it_plain = st->d_items;
+    const int4* it_cpml = st->d_items + st->n_plain;
+    const int n_plain = st->n_plain, n_cpml = st->n_items - st->n_plain;
+    cudaStream_t sc = s;  // stream of the cpml class
+    if (cp && n_plain > 0 && n_cpml > 0) {
+        if (!st->side) {
+            PC_CUDA_CHECK(cudaStreamCreateWithFlags(&st->side, cudaStreamNonBlocking));
+            PC_CUDA_CHECK(cudaEventCreateWithFlags(&st->fork, cudaEventDisableTiming));
+            PC_CUDA_CHECK(cudaEventCreateWithFlags(&st->join, cudaEventDisableTiming));
+        }
+        PC_CUDA_CHECK(cudaEventRecord(st->fork, s));
+        PC_CUDA_CHECK(cudaStreamWaitEvent(st->side, st->fork, 0));
+        sc = st->side;
+    }
     int rc;
-    const int key = (cp ? 4 : 0) | (hc ? 2 : 0) | (ca ? 1 : 0);
-    switch (key) {
-        case 0: rc = launch_variant<T, TY, TZ, S, false, false, false>(c, s, a, p, m, smem, st); break;
-        case 1: rc = launch_variant<T, TY, TZ, S, false, false, true>(c, s, a, p, m, smem, st); break;
-        case 2: rc = launch_variant<T, TY, TZ, S, false, true, false>(c, s, a, p, m, smem, st); break;
-        case 3: rc = launch_variant<T, TY, TZ, S, false, true, true>(c, s, a, p, m, smem, st); break;
-        case 4: rc = launch_variant<T, TY, TZ, S, true, false, false>(c, s, a, p, m, smem, st); break;
-        case 5: rc = launch_variant<T, TY, TZ, S, true, false, true>(c, s, a, p, m, smem, st); break;
-        case 6: rc = launch_variant<T, TY, TZ, S, true, true, false>(c, s, a, p, m, smem, st); break;
-        default: rc = launch_variant<T, TY, TZ, S, true, true, true>(c, s, a, p, m, smem, st); break;
+    // the plain class (no CPML code) on the caller's stream
+    const int kp = (hc ? 2 : 0) | (ca ? 1 : 0);
+    switch (kp) {
+        case 0: rc = launch_variant<T, TY, TZ, S, false, false, false>(s, a, p, m, smem, it_plain, n_plain); break;
+        case 1: rc = launch_variant<T, TY, TZ, S, false, false, true>(s, a, p, m, smem, it_plain, n_plain); break;
+        case 2: rc = launch_variant<T, TY, TZ, S, false, true, false>(s, a, p, m, smem, it_plain, n_plain); break;
+        default: rc = launch_variant<T, TY, TZ, S, false, true, true>(s, a, p, m, smem, it_plain, n_plain); break;
     }
     if (rc) return rc;
+    if (cp) {
+        switch (kp) {
+            case 0: rc = launch_variant<T, TY, TZ, S, true, false, false>(sc, a, p, m, smem, it_cpml, n_cpml); break;
+            case 1: rc = launch_variant<T, TY, TZ, S, true, false, true>(sc, a, p, m, smem, it_cpml, n_cpml); break;
+            case 2: rc = launch_variant<T, TY, TZ, S, true, true, false>(sc, a, p, m, smem, it_cpml, n_cpml); break;
+            default: rc = launch_variant<T, TY, TZ, S, true, true, true>(sc, a, p, m, smem, it_cpml, n_cpml); break;
+        }
+        if (rc) return rc;
+        if (sc != s) {
+            PC_CUDA_CHECK(cudaEventRecord(st->join, sc));
+            PC_CUDA_CHECK(cudaStreamWaitEvent(s, st->join, 0));
+        }
+        ++c->launches;
+    }
     ++c->launches;
     c->cur = out;
     return PC_OK;
@@ -766,7 +837,13 @@ int launch_fused_step(pc_ctx* c, cudaStream_t s) {
 }
 
 void destroy_fused_state(pc_ctx* c) {
-    if (c->fused_state) cudaFree(static_cast<FusedState*>(c->fused_state)->d_items);
+    if (c->fused_state) {
+        FusedState* st = static_cast<FusedState*>(c->fused_state);
+        cudaFree(st->d_items);
+        if (st->side) cudaStreamDestroy(st->side);
+        if (st->fork) cudaEventDestroy(st->fork);
+        if (st->join) cudaEventDestroy(st->join);
+    }
     delete static_cast<FusedState*>(c->fused_state);
     c->fused_state = nullptr;
 }

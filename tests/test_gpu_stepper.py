@@ -210,3 +210,33 @@ def test_fused_chunking_with_cpml_slabs(torch, chunk):
     for c in COMPS:
         assert rel_l2(out[c], o.F[c]) <= 1e-5, c
     eng.close()
+
+
+@pytest.mark.parametrize("chunk", [0, 9])
+def test_fused_plain_and_cpml_item_classes(torch, chunk):
+    """Both item classes in one step (tiles clear of every slab run the variant
+    without CPML code, concurrently with the slab tiles), with tiles whose +1 H
+    halo row/column lands exactly on the first slab row/column (ny - t = 48 + 16,
+    nz - t = 64 + 32)."""
+    from prismo_gb300 import _lib
+    from prismo_gb300.pml import PMLParams
+
+    g, mats, init = _random_case((80, 72, 104), False, seed=11, lossy=False)
+    dt = g.suggest_dt(0.5)
+    o = O.OracleFDTD(g, dt, mats, cpml_layers=8)
+    for c in COMPS:
+        o.F[c][...] = init[c]
+    o.run(30)
+    for prec in ("fp64", "fp32"):
+        eng = make_engine(g.dims, g.spacing, dt, False, precision=prec, sched="fused", material_arrays=mats,
+                          pml=PMLParams(thickness=8))
+        if chunk:
+            _lib.check(eng.lib.pc_set_tuning(eng.ctx, _lib.PC_TUNE_FUSED_CHUNK, chunk))
+        load_fields(eng, init, torch)
+        eng.step(30)
+        out = read_fields(eng)
+        assert eng.check_status() == 0
+        for c in COMPS:
+            tol = 1e-12 if prec == "fp64" else 1e-5
+            assert rel_l2(out[c], o.F[c]) <= tol, (prec, c, rel_l2(out[c], o.F[c]))
+        eng.close()
