@@ -225,7 +225,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--dims", type=int, default=None,
                     help="cube edge for a reduced profiling case (default: the 256^3 workload)")
-    ap.add_argument("--workload", default="3d", choices=["3d", "dispersive", "sweep", "surrogate"],
+    ap.add_argument("--workload", default="3d", choices=["3d", "2d", "dispersive", "sweep", "surrogate"],
                     help="3d: the headline 256^3 CPML workload; dispersive: 384x384x192 Drude-Lorentz + TFSF + "
                          "64-frequency DFT planes; sweep: 64 batched couplers; surrogate: train + held-out pipeline")
     ap.add_argument("--designs", type=int, default=64, help="designs per batched sweep")
@@ -430,9 +430,77 @@ def run_other(args):
     peak, peak_kind = measured_peaks()
     if args.workload == "dispersive":
         return run_dispersive(args, peak, peak_kind)
+    if args.workload == "2d":
+        return run_2d(args)
     if args.workload == "sweep":
         return run_sweep(args, cpu, peak, peak_kind)
     return run_surrogate(args, cpu)
+
+
+def run_2d(args):
+    """The 2D TE drop-in configuration: 500 x 250 total cells, 20-cell CPML, slab
+    waveguide, soft Ez line source, 11-frequency DFT line, 3000 steps (one bench
+    step = the whole run from zero fields).  The grid (3 MB) lives in L2: the
+    metric is steps/s and Gcell/s, not an HBM roofline."""
+    import torch
+
+    from prismo_gb300.engine import FDTDEngine
+    from prismo_gb300.grid import YeeGrid
+    from prismo_gb300.pml import PMLParams
+    from prismo_gb300.sources import GaussianPulse
+    from prismo_gb300.workloads import CONFIG_2D, config_2d_layout
+
+    cfg = CONFIG_2D
+    g = YeeGrid.from_total(cfg["dims"], cfg["dx"], cfg["cpml"])
+    dt = g.suggest_time_step(cfg["courant"])
+    eps, src, mon, freqs = config_2d_layout()
+    n = cfg["steps"]
+    wf = GaussianPulse(cfg["pulse_f0"], cfg["pulse_width"])
+    amps = np.asarray(wf(np.cumsum(np.full(n, dt))), dtype=np.float64)[:, None]
+    eng = FDTDEngine(g.dimensions, g.spacing, dt, is_2d=True, precision="fp32", material_arrays={"eps_rel": eps},
+                     pml=PMLParams(thickness=cfg["cpml"]))
+    eng.add_source("Ez", eng.offsets("Ez", src), None, wf)
+    eng.add_dft("Ez", eng.offsets("Ez", mon), freqs, t0=dt)
+
+    def one():
+        for s_ in eng.sets:
+            s_.zero_()
+        for p_ in eng.psi:
+            p_.zero_()
+        eng.step(n, amps)
+
+    for _ in range(max(args.warmup, 3)):
+        one()
+    eng.synchronize()
+    n0 = eng.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(eng.stream)
+    for _ in range(args.steps):
+        one()
+    ev1.record(eng.stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    cells = float(np.prod(g.dimensions))
+    # CPU baseline: the float64 oracle, 50 steps of the same grid, 1 thread
+    from oracle import fdtd64 as O
+
+    go = O.OracleGrid.from_total(*cfg["dims"], cfg["dx"], cfg["cpml"])
+    o = O.OracleFDTD(go, dt, {"eps_rel": eps}, cpml_layers=cfg["cpml"])
+    o.add_source("Ez", src, O.gaussian_pulse(cfg["pulse_f0"], cfg["pulse_width"]))
+    o.add_dft("Ez", mon, freqs)
+    o.run(2)
+    t0 = time.perf_counter()
+    o.run(50)
+    cpu_s = (time.perf_counter() - t0) / 50
+    _line(metric="Gcell-updates/s", value=cells * n / (ms / 1e3) / 1e9, unit="Gcell/s", steps=args.steps,
+          warmup=args.warmup, ms_per_step=ms, dtype="f32",
+          config={"workload": "2d_te_waveguide_500x250: 20-cell CPML, slab waveguide, soft Ez line source, "
+                              "11-frequency DFT line, 3000 steps (L2-resident grid)",
+                  "time_steps_per_s": n / (ms / 1e3), "l2": "grid fits L2 (launch/latency bound)"},
+          cpu_baseline={"value": cells / cpu_s / 1e9, "unit": "Gcell/s", "cores": 1, "kind": "port",
+                        "sample": f"50 of 3000 steps, float64 oracle, {cpu_s * 1e3:.1f} ms/step"},
+          gpu_launches=eng.launch_count() - n0)
+    eng.close()
 
 
 def run_dispersive(args, peak, peak_kind):

@@ -33,6 +33,7 @@ namespace {
 
 constexpr int BNT = 512;  // threads per CTA
 constexpr int RING_T = 16;
+constexpr int PC_MAX_BATCH_CPML = 100;  // slab thickness limit (shared-memory coefficient table)
 
 struct BInst {  // device copy of one instance (128 bytes)
     int nx, ny, pitch, src_x;
@@ -85,29 +86,51 @@ struct BShape {
     static constexpr int RX = TX + 2 * K, RY = TY + 2 * K, RC = RX * RY, M = (RC + BNT - 1) / BNT;
     // two CTAs per SM (64 registers a thread) while the per-cell registers fit
     static constexpr int MINB = M <= 6 ? 2 : 1;
-    // Ez, Hx, Hy and the four CPML auxiliaries of the region
-    static constexpr size_t SMEM = 7 * sizeof(float) * RC;
+    // Ez, Hx, Hy with RY + 1 guard cells on both sides (the fast path reads
+    // neighbours of edge cells without tests), then the four CPML auxiliaries
+    static constexpr int GUARD = RY + 1;
+    static constexpr int FS = RC + 2 * GUARD;
+    static constexpr size_t SMEM = sizeof(float) * (3 * FS + 4 * RC);
 };
+
+// The update formulas with explicit rounding (no contraction choices left to the
+// compiler), so that the fast and the general path -- and therefore every tile
+// shape -- give bit-identical fields.  Same operations as split_h2 / split_e2.
+__device__ __forceinline__ float cpml_d(float d, float b, float a, float kinv, float& psi) {
+    psi = __fmaf_rn(b, psi, __fmul_rn(a, d));
+    return __fmaf_rn(d, kinv, psi);
+}
+__device__ __forceinline__ float h_minus(float h, float d, float da, float db) {  // Hx: da h - db d
+    return __fmaf_rn(-db, d, __fmul_rn(da, h));
+}
+__device__ __forceinline__ float h_plus(float h, float d, float da, float db) {  // Hy: da h + db d
+    return __fmaf_rn(db, d, __fmul_rn(da, h));
+}
+__device__ __forceinline__ float diff(float a, float b, float inv) { return __fmul_rn(__fsub_rn(a, b), inv); }
 
 template <int TX, int TY, int K>
 __global__ void __launch_bounds__(BNT, BShape<TX, TY, K>::MINB) batch2d_pass(BPass P) {
-    constexpr int RX = TX + 2 * K, RY = TY + 2 * K, RC = RX * RY;
-    constexpr int M = BShape<TX, TY, K>::M;
+    using SH = BShape<TX, TY, K>;
+    constexpr int RX = SH::RX, RY = SH::RY, RC = SH::RC;
+    constexpr int M = SH::M;
     extern __shared__ float smem[];
-    float* sE = smem;
-    float* sX = sE + RC;
-    float* sY = sX + RC;
-    float* qYX = sY + RC;  // psi of Hy (x-derivative)
-    float* qZX = qYX + RC; // psi of Ez (x-derivative)
-    float* qXY = qZX + RC; // psi of Hx (y-derivative)
-    float* qZY = qXY + RC; // psi of Ez (y-derivative)
+    float* sE = smem + SH::GUARD;
+    float* sX = sE + SH::FS;
+    float* sY = sX + SH::FS;
+    float* qYX = smem + 3 * SH::FS;  // psi of Hy (x-derivative)
+    float* qZX = qYX + RC;           // psi of Ez (x-derivative)
+    float* qXY = qZX + RC;           // psi of Hx (y-derivative)
+    float* qZY = qXY + RC;           // psi of Ez (y-derivative)
     __shared__ BInst sI;
+    __shared__ float sC[3 * 2 * PC_MAX_BATCH_CPML];  // b, a, 1/kappa by slab index
     const int tid = threadIdx.x;
     const long long base = P.live ? *P.step : 0;
     const int t = P.t;
-    const float* sb = P.slab;
-    const float* sa = P.slab + 2 * t;
-    const float* sk = P.slab + 4 * t;
+    for (int q = tid; q < 6 * t; q += BNT) sC[q] = P.slab[q];
+    const float* sb = sC;
+    const float* sa = sC + 2 * t;
+    const float* sk = sC + 4 * t;
+    const float idx_ = P.inv_dx, idy = P.inv_dy, da = P.da, db = P.db;
 
     for (int w = blockIdx.x; w < P.nitems; w += gridDim.x) {
         const int4 it = P.items[w];
@@ -122,13 +145,68 @@ __global__ void __launch_bounds__(BNT, BShape<TX, TY, K>::MINB) batch2d_pass(BPa
         const float* fin = P.fin + sI.f_off;
         float* fout = P.fout + sI.f_off;
         const float* cbp = P.cb + sI.c_off;
-        const int64_t pyx = sI.p_off;                                // psi Hy (x-derivative), [2t][pitch]
-        const int64_t pzx = pyx + 2 * (int64_t)t * pitch;            // psi Ez (x-derivative), [2t][pitch]
-        const int64_t pxy = pyx + 4 * (int64_t)t * pitch;            // psi Hx (y-derivative), [nx][2t]
-        const int64_t pzy = pxy + 2 * (int64_t)t * nx;               // psi Ez (y-derivative), [nx][2t]
-
-        unsigned fl[M];
         float cbr[M];
+
+        if ((it.w & 3) == 0) {
+            // ---- fast path: the region lies inside the instance, clear of the CPML,
+            // the source column and the port lines: every cell updates every component
+            // (edge cells read guard or wrapped neighbours; their results fall outside
+            // the shrinking valid region and are never stored)
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int idx = tid + m * BNT;
+                cbr[m] = 0.f;
+                if (idx >= RC) continue;
+                const int r = idx / RY, c = idx - (idx / RY) * RY;
+                const int64_t o = (int64_t)(gx0 + r) * pitch + (gy0 + c);
+                sE[idx] = fin[o];
+                sX[idx] = fin[nxp + o];
+                sY[idx] = fin[2 * nxp + o];
+                cbr[m] = cbp[o];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    const int idx = tid + m * BNT;
+                    if (idx >= RC) continue;
+                    const float e = sE[idx];
+                    sX[idx] = h_minus(sX[idx], diff(e, sE[idx - 1], idy), da, db);
+                    sY[idx] = h_plus(sY[idx], diff(e, sE[idx - RY], idx_), da, db);
+                }
+                __syncthreads();
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    const int idx = tid + m * BNT;
+                    if (idx >= RC) continue;
+                    const float hx = sX[idx], hy = sY[idx];
+                    const float c1 = diff(sY[idx + RY], hy, idx_);
+                    const float c2 = diff(sX[idx + 1], hx, idy);
+                    sE[idx] = __fmaf_rn(cbr[m], __fsub_rn(c1, c2), sE[idx]);
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int idx = tid + m * BNT;
+                if (idx >= RC) continue;
+                const int r = idx / RY, c = idx - (idx / RY) * RY;
+                if (r < K || r >= K + TX || c < K || c >= K + TY) continue;
+                const int64_t o = (int64_t)(gx0 + r) * pitch + (gy0 + c);
+                fout[o] = sE[idx];
+                fout[nxp + o] = sX[idx];
+                fout[2 * nxp + o] = sY[idx];
+            }
+            continue;
+        }
+
+        // ---- general path: per-cell validity, CPML, source and port samples ----
+        const int64_t pyx = sI.p_off;                      // psi Hy (x-derivative), [2t][pitch]
+        const int64_t pzx = pyx + 2 * (int64_t)t * pitch;  // psi Ez (x-derivative), [2t][pitch]
+        const int64_t pxy = pyx + 4 * (int64_t)t * pitch;  // psi Hx (y-derivative), [nx][2t]
+        const int64_t pzy = pxy + 2 * (int64_t)t * nx;     // psi Ez (y-derivative), [nx][2t]
+        unsigned fl[M];
 #pragma unroll
         for (int m = 0; m < M; ++m) {
             const int idx = tid + m * BNT;
@@ -184,24 +262,16 @@ __global__ void __launch_bounds__(BNT, BShape<TX, TY, K>::MINB) batch2d_pass(BPa
                 const int idx = tid + m * BNT;
                 const unsigned f = fl[m];
                 if (f & F_HX) {
-                    float cy = (sE[idx] - sE[idx - 1]) * P.inv_dy;
+                    float cy = diff(sE[idx], sE[idx - 1], idy);
                     const unsigned q = (f >> 16) & 255u;
-                    if (cp && q != 255u) {
-                        const float ps = sb[q] * qXY[idx] + sa[q] * cy;
-                        qXY[idx] = ps;
-                        cy = cy * sk[q] + ps;
-                    }
-                    sX[idx] = P.da * sX[idx] - P.db * cy;
+                    if (cp && q != 255u) cy = cpml_d(cy, sb[q], sa[q], sk[q], qXY[idx]);
+                    sX[idx] = h_minus(sX[idx], cy, da, db);
                 }
                 if (f & F_HY) {
-                    float cx = (sE[idx] - sE[idx - RY]) * P.inv_dx;
+                    float cx = diff(sE[idx], sE[idx - RY], idx_);
                     const unsigned q = (f >> 8) & 255u;
-                    if (cp && q != 255u) {
-                        const float ps = sb[q] * qYX[idx] + sa[q] * cx;
-                        qYX[idx] = ps;
-                        cx = cx * sk[q] + ps;
-                    }
-                    sY[idx] = P.da * sY[idx] + P.db * cx;
+                    if (cp && q != 255u) cx = cpml_d(cx, sb[q], sa[q], sk[q], qYX[idx]);
+                    sY[idx] = h_plus(sY[idx], cx, da, db);
                 }
             }
             __syncthreads();
@@ -216,26 +286,17 @@ __global__ void __launch_bounds__(BNT, BShape<TX, TY, K>::MINB) batch2d_pass(BPa
                 const int idx = tid + m * BNT;
                 const unsigned f = fl[m];
                 if (f & F_EZ) {
-                    float c1 = (sY[idx + RY] - sY[idx]) * P.inv_dx;
-                    float c2 = (sX[idx + 1] - sX[idx]) * P.inv_dy;
+                    float c1 = diff(sY[idx + RY], sY[idx], idx_);
+                    float c2 = diff(sX[idx + 1], sX[idx], idy);
                     if (cp) {
                         const unsigned qx = (f >> 8) & 255u, qy = (f >> 16) & 255u;
-                        if (qx != 255u) {
-                            const float ps = sb[qx] * qZX[idx] + sa[qx] * c1;
-                            qZX[idx] = ps;
-                            c1 = c1 * sk[qx] + ps;
-                        }
-                        if (qy != 255u) {
-                            const float ps = sb[qy] * qZY[idx] + sa[qy] * c2;
-                            qZY[idx] = ps;
-                            c2 = c2 * sk[qy] + ps;
-                        }
+                        if (qx != 255u) c1 = cpml_d(c1, sb[qx], sa[qx], sk[qx], qZX[idx]);
+                        if (qy != 255u) c2 = cpml_d(c2, sb[qy], sa[qy], sk[qy], qZY[idx]);
                     }
-                    float e = sE[idx];
-                    e = e + cbr[m] * (c1 - c2);
+                    float e = __fmaf_rn(cbr[m], __fsub_rn(c1, c2), sE[idx]);
                     if (P.live && (f & F_SRC)) {
                         const int gj = gy0 + (idx - (idx / RY) * RY);
-                        e = e + static_cast<float>(P.w[sI.w_off + (gj - sI.src_y0)] * amp);
+                        e = __fadd_rn(e, static_cast<float>(P.w[sI.w_off + (gj - sI.src_y0)] * amp));
                     }
                     sE[idx] = e;
                     if (P.live && P.ring && (f & F_PORT)) {
@@ -364,8 +425,17 @@ int build_items(pc_batch* b, int v) {
         for (int x0 = 0; x0 < nx; x0 += V.tx)
             for (int y0 = 0; y0 < ny; y0 += V.ty) {
                 const int ax0 = x0 - K, ax1 = x0 + V.tx + K, ay0 = y0 - K, ay1 = y0 + V.ty + K;
-                const bool cp = t > 0 && (ax0 < t || ax1 > nx - t || ay0 < t || ay1 > ny - t);
-                items.push_back(make_int4(n, x0, y0, cp ? 1 : 0));
+                // bit 0: the region (with its halo) reaches the CPML or the instance edge
+                // bit 1: it holds source or port cells (both take the general path)
+                const bool cp = ax0 < t || ax1 > nx - t || ay0 < t || ay1 > ny - t || ax0 < 0 || ay0 < 0 ||
+                                ax1 > nx || ay1 > ny;
+                const pc_batch_instance& d = b->desc[n];
+                bool special = d.src_n > 0 && d.src_x >= ax0 && d.src_x < ax1 && d.src_y0 < ay1 &&
+                               d.src_y0 + d.src_n > ay0;
+                for (int q = 0; q < d.nport; ++q)
+                    special = special || (d.port_x[q] >= ax0 && d.port_x[q] < ax1 && d.port_y0[q] < ay1 &&
+                                          d.port_y0[q] + d.port_n[q] > ay0);
+                items.push_back(make_int4(n, x0, y0, (cp ? 1 : 0) | (special ? 2 : 0)));
                 const int cx = std::min(nx, x0 + V.tx) - x0, cy = std::min(ny, y0 + V.ty) - y0;
                 cost.push_back((float)(cx * cy) * (cp ? 1.5f : 1.0f) + 0.25f * V.tx * V.ty);
             }
