@@ -653,7 +653,11 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
     cudaStream_t sc = s;  // stream of the cpml class
     if (cp && n_plain > 0 && n_cpml > 0) {
         if (!st->side) {
-            PC_CUDA_CHECK(cudaStreamCreateWithFlags(&st->side, cudaStreamNonBlocking));
+            // highest priority: the slab items are the long ones, so their CTAs are
+            // dispatched first and the plain items fill in behind them
+            int lo = 0, hi = 0;
+            PC_CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+            PC_CUDA_CHECK(cudaStreamCreateWithPriority(&st->side, cudaStreamNonBlocking, hi));
             PC_CUDA_CHECK(cudaEventCreateWithFlags(&st->fork, cudaEventDisableTiming));
             PC_CUDA_CHECK(cudaEventCreateWithFlags(&st->join, cudaEventDisableTiming));
         }
@@ -662,16 +666,8 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
         sc = st->side;
     }
     int rc;
-    // the plain class (no CPML code) on the caller's stream
     const int kp = (hc ? 2 : 0) | (ca ? 1 : 0);
-    switch (kp) {
-        case 0: rc = launch_variant<T, TY, TZ, S, false, false, false>(s, a, p, m, smem, it_plain, n_plain); break;
-        case 1: rc = launch_variant<T, TY, TZ, S, false, false, true>(s, a, p, m, smem, it_plain, n_plain); break;
-        case 2: rc = launch_variant<T, TY, TZ, S, false, true, false>(s, a, p, m, smem, it_plain, n_plain); break;
-        default: rc = launch_variant<T, TY, TZ, S, false, true, true>(s, a, p, m, smem, it_plain, n_plain); break;
-    }
-    if (rc) return rc;
-    if (cp) {
+    if (cp) {  // the slab class first (see the side stream's priority)
         switch (kp) {
             case 0: rc = launch_variant<T, TY, TZ, S, true, false, false>(sc, a, p, m, smem, it_cpml, n_cpml); break;
             case 1: rc = launch_variant<T, TY, TZ, S, true, false, true>(sc, a, p, m, smem, it_cpml, n_cpml); break;
@@ -679,13 +675,21 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
             default: rc = launch_variant<T, TY, TZ, S, true, true, true>(sc, a, p, m, smem, it_cpml, n_cpml); break;
         }
         if (rc) return rc;
-        if (sc != s) {
-            PC_CUDA_CHECK(cudaEventRecord(st->join, sc));
-            PC_CUDA_CHECK(cudaStreamWaitEvent(s, st->join, 0));
-        }
-        ++c->launches;
+        if (n_cpml > 0) ++c->launches;
     }
-    ++c->launches;
+    // the plain class (no CPML code) on the caller's stream
+    switch (kp) {
+        case 0: rc = launch_variant<T, TY, TZ, S, false, false, false>(s, a, p, m, smem, it_plain, n_plain); break;
+        case 1: rc = launch_variant<T, TY, TZ, S, false, false, true>(s, a, p, m, smem, it_plain, n_plain); break;
+        case 2: rc = launch_variant<T, TY, TZ, S, false, true, false>(s, a, p, m, smem, it_plain, n_plain); break;
+        default: rc = launch_variant<T, TY, TZ, S, false, true, true>(s, a, p, m, smem, it_plain, n_plain); break;
+    }
+    if (rc) return rc;
+    if (sc != s) {
+        PC_CUDA_CHECK(cudaEventRecord(st->join, sc));
+        PC_CUDA_CHECK(cudaStreamWaitEvent(s, st->join, 0));
+    }
+    if (n_plain > 0) ++c->launches;
     c->cur = out;
     return PC_OK;
 }
