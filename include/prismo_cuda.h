@@ -287,9 +287,10 @@ void pc_batch_destroy(pc_batch* b);
 /* ------------------------------------------------------------------------- *
  * Surrogate network.  No counterpart in the reference (it has no learned
  * model): an ensemble of `members` MLPs dims[0] -> dims[1] -> dims[2] -> dims[3]
- * -> dims[4] with SiLU after the three hidden layers, bf16 weights and
- * activations on the tensor cores with float32 accumulation, float32 master
- * parameters and Adam.  dims[0] <= 32 (padded to 32 internally); dims[1..4]
+ * -> dims[4] with SiLU after the three hidden layers, bf16 weights on the
+ * tensor cores with float32 accumulation (forward activations as bf16 hi/lo
+ * pairs, backward in bf16), float32 master parameters and Adam.
+ * dims[0] <= 32 (padded to 32 internally); dims[1..4]
  * multiples of 32.  Batches: 1..max_batch rows for the forward pass, multiples
  * of 32 for training; max_batch a multiple of 32.
  *

@@ -83,12 +83,13 @@ __device__ __forceinline__ int slab_idx(int idx, int n, int t) {
 // per-thread cells of a (TX + 2K) x (TY + 2K) region
 template <int TX, int TY, int K>
 struct BShape {
+    static_assert(TY % 2 == 0, "the fast path moves y-adjacent pairs");
     static constexpr int RX = TX + 2 * K, RY = TY + 2 * K, RC = RX * RY, M = (RC + BNT - 1) / BNT;
     // two CTAs per SM (64 registers a thread) while the per-cell registers fit
-    static constexpr int MINB = M <= 6 ? 2 : 1;
-    // Ez, Hx, Hy with RY + 1 guard cells on both sides (the fast path reads
+    static constexpr int MINB = M <= 8 ? 2 : 1;
+    // Ez, Hx, Hy with RY + 2 guard cells on both sides (the fast path reads
     // neighbours of edge cells without tests), then the four CPML auxiliaries
-    static constexpr int GUARD = RY + 1;
+    static constexpr int GUARD = RY + 2;  // even: the float2 accesses stay 8-byte aligned
     static constexpr int FS = RC + 2 * GUARD;
     static constexpr size_t SMEM = sizeof(float) * (3 * FS + 4 * RC);
 };
@@ -145,61 +146,101 @@ __global__ void __launch_bounds__(BNT, BShape<TX, TY, K>::MINB) batch2d_pass(BPa
         const float* fin = P.fin + sI.f_off;
         float* fout = P.fout + sI.f_off;
         const float* cbp = P.cb + sI.c_off;
-        float cbr[M];
-
         if ((it.w & 3) == 0) {
             // ---- fast path: the region lies inside the instance, clear of the CPML,
             // the source column and the port lines: every cell updates every component
             // (edge cells read guard or wrapped neighbours; their results fall outside
-            // the shrinking valid region and are never stored)
+            // the shrinking valid region and are never stored).  Each thread owns pairs
+            // of y-adjacent cells and moves them as float2.
+            constexpr int NP = RC / 2;
+            constexpr int MP = (NP + BNT - 1) / BNT;
+            float2 cb2[MP];
 #pragma unroll
-            for (int m = 0; m < M; ++m) {
-                const int idx = tid + m * BNT;
-                cbr[m] = 0.f;
-                if (idx >= RC) continue;
+            for (int m = 0; m < MP; ++m) {
+                const int q = tid + m * BNT;
+                cb2[m] = make_float2(0.f, 0.f);
+                if (q >= NP) continue;
+                const int idx = 2 * q;
                 const int r = idx / RY, c = idx - (idx / RY) * RY;
                 const int64_t o = (int64_t)(gx0 + r) * pitch + (gy0 + c);
-                sE[idx] = fin[o];
-                sX[idx] = fin[nxp + o];
-                sY[idx] = fin[2 * nxp + o];
-                cbr[m] = cbp[o];
+                if (K % 2 == 0) {  // o is even: 8-byte aligned pairs
+                    *reinterpret_cast<float2*>(sE + idx) = *reinterpret_cast<const float2*>(fin + o);
+                    *reinterpret_cast<float2*>(sX + idx) = *reinterpret_cast<const float2*>(fin + nxp + o);
+                    *reinterpret_cast<float2*>(sY + idx) = *reinterpret_cast<const float2*>(fin + 2 * nxp + o);
+                    cb2[m] = *reinterpret_cast<const float2*>(cbp + o);
+                } else {
+                    sE[idx] = fin[o];
+                    sE[idx + 1] = fin[o + 1];
+                    sX[idx] = fin[nxp + o];
+                    sX[idx + 1] = fin[nxp + o + 1];
+                    sY[idx] = fin[2 * nxp + o];
+                    sY[idx + 1] = fin[2 * nxp + o + 1];
+                    cb2[m] = make_float2(cbp[o], cbp[o + 1]);
+                }
             }
             __syncthreads();
 #pragma unroll
             for (int s = 0; s < K; ++s) {
 #pragma unroll
-                for (int m = 0; m < M; ++m) {
-                    const int idx = tid + m * BNT;
-                    if (idx >= RC) continue;
-                    const float e = sE[idx];
-                    sX[idx] = h_minus(sX[idx], diff(e, sE[idx - 1], idy), da, db);
-                    sY[idx] = h_plus(sY[idx], diff(e, sE[idx - RY], idx_), da, db);
+                for (int m = 0; m < MP; ++m) {
+                    const int q = tid + m * BNT;
+                    if (q >= NP) continue;
+                    const int idx = 2 * q;
+                    const float2 e = *reinterpret_cast<const float2*>(sE + idx);
+                    const float2 eu = *reinterpret_cast<const float2*>(sE + idx - RY);
+                    const float em = sE[idx - 1];
+                    float2 hx = *reinterpret_cast<const float2*>(sX + idx);
+                    float2 hy = *reinterpret_cast<const float2*>(sY + idx);
+                    hx.x = h_minus(hx.x, diff(e.x, em, idy), da, db);
+                    hx.y = h_minus(hx.y, diff(e.y, e.x, idy), da, db);
+                    hy.x = h_plus(hy.x, diff(e.x, eu.x, idx_), da, db);
+                    hy.y = h_plus(hy.y, diff(e.y, eu.y, idx_), da, db);
+                    *reinterpret_cast<float2*>(sX + idx) = hx;
+                    *reinterpret_cast<float2*>(sY + idx) = hy;
                 }
                 __syncthreads();
 #pragma unroll
-                for (int m = 0; m < M; ++m) {
-                    const int idx = tid + m * BNT;
-                    if (idx >= RC) continue;
-                    const float hx = sX[idx], hy = sY[idx];
-                    const float c1 = diff(sY[idx + RY], hy, idx_);
-                    const float c2 = diff(sX[idx + 1], hx, idy);
-                    sE[idx] = __fmaf_rn(cbr[m], __fsub_rn(c1, c2), sE[idx]);
+                for (int m = 0; m < MP; ++m) {
+                    const int q = tid + m * BNT;
+                    if (q >= NP) continue;
+                    const int idx = 2 * q;
+                    const float2 hx = *reinterpret_cast<const float2*>(sX + idx);
+                    const float2 hy = *reinterpret_cast<const float2*>(sY + idx);
+                    const float2 hyd = *reinterpret_cast<const float2*>(sY + idx + RY);
+                    const float hxn = sX[idx + 2];
+                    float2 e = *reinterpret_cast<const float2*>(sE + idx);
+                    e.x = __fmaf_rn(cb2[m].x, __fsub_rn(diff(hyd.x, hy.x, idx_), diff(hx.y, hx.x, idy)), e.x);
+                    e.y = __fmaf_rn(cb2[m].y, __fsub_rn(diff(hyd.y, hy.y, idx_), diff(hxn, hx.y, idy)), e.y);
+                    *reinterpret_cast<float2*>(sE + idx) = e;
                 }
                 __syncthreads();
             }
 #pragma unroll
-            for (int m = 0; m < M; ++m) {
-                const int idx = tid + m * BNT;
-                if (idx >= RC) continue;
+            for (int m = 0; m < MP; ++m) {
+                const int q = tid + m * BNT;
+                if (q >= NP) continue;
+                const int idx = 2 * q;
                 const int r = idx / RY, c = idx - (idx / RY) * RY;
-                if (r < K || r >= K + TX || c < K || c >= K + TY) continue;
+                if (r < K || r >= K + TX) continue;
                 const int64_t o = (int64_t)(gx0 + r) * pitch + (gy0 + c);
-                fout[o] = sE[idx];
-                fout[nxp + o] = sX[idx];
-                fout[2 * nxp + o] = sY[idx];
+                if (K % 2 == 0) {  // c even, K and TY even: both cells of the pair are in or out
+                    if (c < K || c >= K + TY) continue;
+                    *reinterpret_cast<float2*>(fout + o) = *reinterpret_cast<const float2*>(sE + idx);
+                    *reinterpret_cast<float2*>(fout + nxp + o) = *reinterpret_cast<const float2*>(sX + idx);
+                    *reinterpret_cast<float2*>(fout + 2 * nxp + o) = *reinterpret_cast<const float2*>(sY + idx);
+                } else {
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        if (c + h < K || c + h >= K + TY) continue;
+                        fout[o + h] = sE[idx + h];
+                        fout[nxp + o + h] = sX[idx + h];
+                        fout[2 * nxp + o + h] = sY[idx + h];
+                    }
+                }
             }
             continue;
         }
+        float cbr[M];
 
         // ---- general path: per-cell validity, CPML, source and port samples ----
         const int64_t pyx = sI.p_off;                      // psi Hy (x-derivative), [2t][pitch]

@@ -13,6 +13,12 @@
 // Ensemble members run side by side on gridDim.z.  Parameters are float32
 // masters updated by Adam; the bf16 copies W and W^T the GEMMs read are written
 // by the same Adam kernel.
+//
+// Forward activations (and the network inputs) are kept as a pair of bf16 values
+// a = a_hi + a_lo (a_lo = bf16(a - a_hi)), and each forward product is
+// A_hi W + A_lo W: a single bf16 activation carries 8 significant bits, which
+// put a floor near 1e-3 under the S-parameter error; the pair carries about 16.
+// Weights stay bf16; the backward pass uses a_hi and bf16 gradients.
 #include <cuda_bf16.h>
 
 #include <vector>
@@ -32,6 +38,7 @@ enum { EP_HIDDEN = 0, EP_OUT = 1, EP_BWD = 2, EP_WGRAD = 3 };
 
 struct GemmP {
     const bf16* A;
+    const bf16* A2;  // low part of A (split forward products), same strides
     int64_t lda, sA;
     const bf16* B;
     int64_t ldb, sB;
@@ -43,6 +50,7 @@ struct GemmP {
     const float* zprev;  // bwd: pre-activation of the layer below
     int64_t ldz, sZ;
     bf16* outB;  // activation / gradient, row-major
+    bf16* outB2;  // low part of the activation (forward), same layout
     int64_t ldb2, sOB;
     bf16* outT;  // the same, transposed
     int64_t ldt, sOT;
@@ -64,8 +72,10 @@ __device__ __forceinline__ void epilogue(const GemmP& p, int z, int m, int n, fl
     if (MODE == EP_HIDDEN) {
         const float v = acc + p.bias[z * p.sBias + n];
         p.outF[z * p.sO + (int64_t)m * p.ldo + n] = v;
-        const bf16 a = __float2bfloat16_rn(v * sigm(v));
+        const float av = v * sigm(v);
+        const bf16 a = __float2bfloat16_rn(av);
         p.outB[z * p.sOB + (int64_t)m * p.ldb2 + n] = a;
+        p.outB2[z * p.sOB + (int64_t)m * p.ldb2 + n] = __float2bfloat16_rn(av - __bfloat162float(a));
         p.outT[z * p.sOT + (int64_t)n * p.ldt + m] = a;
     } else if (MODE == EP_OUT) {
         p.outF[z * p.sO + (int64_t)m * p.ldo + n] = acc + p.bias[z * p.sBias + n];
@@ -81,13 +91,16 @@ __device__ __forceinline__ void epilogue(const GemmP& p, int z, int m, int n, fl
 }
 
 // 64x64 tile per CTA, 4 warps of 32x32; K in chunks of 32 staged in shared memory.
-template <int MODE>
+// SPLIT: A is the pair (A, A2) and the product is A B + A2 B.
+template <int MODE, bool SPLIT>
 __global__ void __launch_bounds__(128) mlp_gemm(GemmP p) {
     __shared__ __align__(16) bf16 As[GT][GK + GPAD];
+    __shared__ __align__(16) bf16 As2[SPLIT ? GT : 1][GK + GPAD];
     __shared__ __align__(16) bf16 Bs[GT][GK + GPAD];
     const int z = blockIdx.z;
     const int m0 = blockIdx.y * GT, n0 = blockIdx.x * GT;
     const bf16* A = p.A + z * p.sA;
+    const bf16* A2 = SPLIT ? p.A2 + z * p.sA : nullptr;
     const bf16* B = p.B + z * p.sB;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
@@ -106,10 +119,14 @@ __global__ void __launch_bounds__(128) mlp_gemm(GemmP p) {
         for (int r = 0; r < 2; ++r) {
             const int c = tid + r * 128;
             const int row = c >> 2, col = (c & 3) * 8;
-            uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0);
-            if (m0 + row < p.M) va = *reinterpret_cast<const uint4*>(A + (int64_t)(m0 + row) * p.lda + k0 + col);
+            uint4 va = make_uint4(0, 0, 0, 0), vb = make_uint4(0, 0, 0, 0), va2 = make_uint4(0, 0, 0, 0);
+            if (m0 + row < p.M) {
+                va = *reinterpret_cast<const uint4*>(A + (int64_t)(m0 + row) * p.lda + k0 + col);
+                if (SPLIT) va2 = *reinterpret_cast<const uint4*>(A2 + (int64_t)(m0 + row) * p.lda + k0 + col);
+            }
             if (n0 + row < p.N) vb = *reinterpret_cast<const uint4*>(B + (int64_t)(n0 + row) * p.ldb + k0 + col);
             *reinterpret_cast<uint4*>(&As[row][col]) = va;
+            if (SPLIT) *reinterpret_cast<uint4*>(&As2[row][col]) = va2;
             *reinterpret_cast<uint4*>(&Bs[row][col]) = vb;
         }
         __syncthreads();
@@ -134,6 +151,20 @@ __global__ void __launch_bounds__(128) mlp_gemm(GemmP p) {
             for (int i = 0; i < 2; ++i)
 #pragma unroll
                 for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
+            if (SPLIT) {
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    const int r = wm + i * 16 + g;
+                    af[i][0] = *reinterpret_cast<const uint32_t*>(&As2[r][kk + 2 * t]);
+                    af[i][1] = *reinterpret_cast<const uint32_t*>(&As2[r + 8][kk + 2 * t]);
+                    af[i][2] = *reinterpret_cast<const uint32_t*>(&As2[r][kk + 2 * t + 8]);
+                    af[i][3] = *reinterpret_cast<const uint32_t*>(&As2[r + 8][kk + 2 * t + 8]);
+                }
+#pragma unroll
+                for (int i = 0; i < 2; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
+            }
         }
         __syncthreads();
     }
@@ -149,15 +180,17 @@ __global__ void __launch_bounds__(128) mlp_gemm(GemmP p) {
         }
 }
 
-// x [z][B][din] float -> bf16 [z][B][kp] and [z][kp][B] (member stride Bmax * kp), zero padded
+// x [z][B][din] float -> bf16 pair [z][B][kp] (hi, lo) and hi [z][kp][B] (member stride
+// Bmax * kp), zero padded
 __global__ void mlp_pack(const float* __restrict__ x, int din, int kp, int B, int Bmax, bf16* __restrict__ xb,
-                         bf16* __restrict__ xt) {
+                         bf16* __restrict__ xb2, bf16* __restrict__ xt) {
     const int z = blockIdx.y;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < B * kp; e += gridDim.x * blockDim.x) {
         const int b = e / kp, k = e - (e / kp) * kp;
         const float v = k < din ? x[((int64_t)z * B + b) * din + k] : 0.f;
         const bf16 h = __float2bfloat16_rn(v);
         xb[(int64_t)z * Bmax * kp + e] = h;
+        xb2[(int64_t)z * Bmax * kp + e] = __float2bfloat16_rn(v - __bfloat162float(h));
         xt[(int64_t)z * Bmax * kp + (int64_t)k * B + b] = h;
     }
 }
@@ -272,9 +305,10 @@ struct pc_mlp {
     float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
     bf16* wb[4] = {};
     bf16* wt[4] = {};
-    bf16 *xb = nullptr, *xt = nullptr;
+    bf16 *xb = nullptr, *xb2 = nullptr, *xt = nullptr;
     float* z[3] = {};
-    bf16* act[3] = {};   // inputs of layers 1..3
+    bf16* act[3] = {};   // inputs of layers 1..3 (high part)
+    bf16* act2[3] = {};  // low part
     bf16* actT[3] = {};
     float* y = nullptr;
     bf16* gr[4] = {};    // gradients w.r.t. pre-activations of layers 0..3
@@ -314,10 +348,10 @@ AdamP adam_args(pc_mlp* n) {
     return a;
 }
 
-template <int MODE>
+template <int MODE, bool SPLIT = false>
 int gemm(pc_mlp* n, GemmP p, cudaStream_t s) {
     dim3 grd((p.N + GT - 1) / GT, (p.M + GT - 1) / GT, n->members);
-    mlp_gemm<MODE><<<grd, 128, 0, s>>>(p);
+    mlp_gemm<MODE, SPLIT><<<grd, 128, 0, s>>>(p);
     ++n->launches;
     PC_CUDA_CHECK(cudaGetLastError());
     return PC_OK;
@@ -327,11 +361,12 @@ int gemm(pc_mlp* n, GemmP p, cudaStream_t s) {
 int forward(pc_mlp* n, const float* x, int B, cudaStream_t s) {
     const int M = n->members;
     mlp_pack<<<dim3(std::min(1024, (B * n->kp[0] + 255) / 256), M), 256, 0, s>>>(x, n->din, n->kp[0], B, n->max_batch,
-                                                                                 n->xb, n->xt);
+                                                                                 n->xb, n->xb2, n->xt);
     ++n->launches;
     for (int l = 0; l < 4; ++l) {
         GemmP p{};
         p.A = l == 0 ? n->xb : n->act[l - 1];
+        p.A2 = l == 0 ? n->xb2 : n->act2[l - 1];
         p.lda = n->kp[l];
         p.sA = (int64_t)n->max_batch * n->kp[l];
         p.B = n->wb[l];
@@ -348,17 +383,18 @@ int forward(pc_mlp* n, const float* x, int B, cudaStream_t s) {
             p.ldo = n->nn[l];
             p.sO = (int64_t)n->max_batch * n->nn[l];
             p.outB = n->act[l];
+            p.outB2 = n->act2[l];
             p.ldb2 = n->nn[l];
             p.sOB = (int64_t)n->max_batch * n->nn[l];
             p.outT = n->actT[l];
             p.ldt = B;
             p.sOT = (int64_t)n->max_batch * n->nn[l];
-            rc = gemm<EP_HIDDEN>(n, p, s);
+            rc = gemm<EP_HIDDEN, true>(n, p, s);
         } else {
             p.outF = n->y;
             p.ldo = n->nn[3];
             p.sO = (int64_t)n->max_batch * n->nn[3];
-            rc = gemm<EP_OUT>(n, p, s);
+            rc = gemm<EP_OUT, true>(n, p, s);
         }
         if (rc) return rc;
     }
@@ -450,14 +486,15 @@ int pc_mlp_create(int32_t members, int32_t max_batch, const int32_t dims[5], pc_
     n->P = off;
     const size_t Mb = (size_t)members, B = (size_t)max_batch;
     int rc = mlp_alloc(n, &n->w, Mb * off) || mlp_alloc(n, &n->g, Mb * off) || mlp_alloc(n, &n->m, Mb * off) ||
-             mlp_alloc(n, &n->v, Mb * off) || mlp_alloc(n, &n->xb, Mb * B * 32) || mlp_alloc(n, &n->xt, Mb * B * 32) ||
+             mlp_alloc(n, &n->v, Mb * off) || mlp_alloc(n, &n->xb, Mb * B * 32) || mlp_alloc(n, &n->xb2, Mb * B * 32) ||
+             mlp_alloc(n, &n->xt, Mb * B * 32) ||
              mlp_alloc(n, &n->y, Mb * B * n->nn[3]) || mlp_alloc(n, &n->d_loss, Mb);
     for (int l = 0; l < 4 && !rc; ++l) {
         rc = mlp_alloc(n, &n->wb[l], Mb * n->nn[l] * n->kp[l]) || mlp_alloc(n, &n->wt[l], Mb * n->nn[l] * n->kp[l]) ||
              mlp_alloc(n, &n->gr[l], Mb * B * n->nn[l]) || mlp_alloc(n, &n->grT[l], Mb * B * n->nn[l]);
         if (!rc && l < 3)
             rc = mlp_alloc(n, &n->z[l], Mb * B * n->nn[l]) || mlp_alloc(n, &n->act[l], Mb * B * n->nn[l]) ||
-                 mlp_alloc(n, &n->actT[l], Mb * B * n->nn[l]);
+                 mlp_alloc(n, &n->act2[l], Mb * B * n->nn[l]) || mlp_alloc(n, &n->actT[l], Mb * B * n->nn[l]);
     }
     if (rc) {
         pc_mlp_destroy(n);

@@ -31,8 +31,10 @@ import numpy as np
 from . import _lib
 from . import sweep as SW
 
-DIMS = (3, 256, 256, 256, 512)
 MEMBERS = 4
+N_RFF = 14  # random Fourier pairs per member: 3 + 2 x 14 = 31 network inputs
+RFF_SIGMA = 2.0
+DIMS = (3 + 2 * N_RFF, 256, 256, 256, 512)
 THRESHOLD = 1e-3
 EPOCHS = 2000
 
@@ -107,6 +109,24 @@ def inputs(designs: Sequence[SW.CouplerDesign]) -> np.ndarray:
     return np.stack([2.0 * d.params() - 1.0 for d in designs]).astype(np.float32)
 
 
+def rff_matrices(members: int = MEMBERS, n: int = N_RFF, sigma: float = RFF_SIGMA) -> np.ndarray:
+    """Per-member random projections [members][3][n] (fixed seeds: part of the model)."""
+    return np.stack([np.random.default_rng(100 + m).normal(0.0, sigma, size=(3, n)) for m in range(members)])
+
+
+def embed(x: np.ndarray, B: np.ndarray) -> np.ndarray:
+    """Network inputs of every member: [members][n][3 + 2 nb] = (x, sin(pi x B_m), cos(pi x B_m)).
+
+    Each member sees the three geometry floats through its own random Fourier
+    embedding, so the members interpolate differently between training designs and
+    their spread grows where the data leave the map under-determined (the spread
+    then tracks the error: the fallback test is meaningful)."""
+    x = np.asarray(x, dtype=np.float64)
+    z = np.pi * np.einsum("nk,mkj->mnj", x, B)
+    xs = np.broadcast_to(x[None], (B.shape[0],) + x.shape)
+    return np.concatenate([xs, np.sin(z), np.cos(z)], axis=2).astype(np.float32)
+
+
 # ---------------------------------------------------------------------------
 # the ensemble
 # ---------------------------------------------------------------------------
@@ -152,6 +172,8 @@ class Ensemble:
         self.P = int(self.lib.pc_mlp_param_count(h))
         rng = np.random.default_rng(seed)
         self.set_params(np.stack([_init_params(self.dims, rng) for _ in range(self.members)]))
+        nrff = (self.dims[0] - 3) // 2
+        self.B = rff_matrices(self.members, nrff) if nrff > 0 else None
         self.x_mean = None
         self.y_mean = self.y_std = None
         self._loss = torch.zeros(self.members, dtype=torch.float32, device=self.device)
@@ -211,16 +233,20 @@ class Ensemble:
             lr: float = 2e-3, lr_min: float = 2e-5, seed: int = 1, log_every: int = 0):
         """Train every member on (designs, S) with its own shuffles; cosine decay."""
         torch = self.torch
-        X = inputs(designs)
+        X = self._features(inputs(designs))
         Y = to_real(S * phase_factors(designs, S.shape[-1]))
+        # one scale for every output: the loss then weighs the outputs as the
+        # S-parameter error does (a per-output scale would spend the network on
+        # the near-constant small outputs)
         self.y_mean = Y.mean(axis=0)
-        self.y_std = np.maximum(Y.std(axis=0), 1e-6)
+        self.y_std = np.full(Y.shape[1], max(float(Y.std()), 1e-6))
         Yn = ((Y - self.y_mean) / self.y_std).astype(np.float32)
         dev = self.device
         Xd = torch.as_tensor(X, device=dev)
         Yd = torch.as_tensor(Yn, device=dev)
-        n = X.shape[0]
+        n = X.shape[1]
         batch = min(batch, (n // 32) * 32)
+        mem = torch.arange(self.members, device=dev)[:, None]
         steps_per_epoch = n // batch
         total = epochs * steps_per_epoch
         gen = torch.Generator(device=dev)
@@ -233,7 +259,7 @@ class Ensemble:
             for s in range(steps_per_epoch):
                 idx = perms[:, s * batch:(s + 1) * batch]
                 lr_s = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * step / total))
-                loss = self.train_step_raw(Xd[idx], Yd[idx], lr_s)
+                loss = self.train_step_raw(Xd[mem, idx], Yd[idx], lr_s)
                 step += 1
             if log_every and (ep % log_every == 0 or ep == epochs - 1):
                 history.append((ep, loss.cpu().numpy().copy()))
@@ -242,15 +268,20 @@ class Ensemble:
         self.train_steps = step
         return history
 
+    def _features(self, x: np.ndarray) -> np.ndarray:
+        """[members][n][din] network inputs for geometry x [n][3]."""
+        if self.B is None:
+            return np.ascontiguousarray(np.broadcast_to(x[None], (self.members,) + x.shape), dtype=np.float32)
+        return embed(x, self.B)
+
     def predict(self, designs: Sequence[SW.CouplerDesign], nfreq: int = SW.NFREQ):
         """Ensemble mean S [n][4][nf], spread [n] and per-member S [members][n][4][nf]."""
         torch = self.torch
-        X = inputs(designs)
-        n = X.shape[0]
+        X = self._features(inputs(designs))
+        n = X.shape[1]
         outs = []
         for q in range(0, n, self.max_batch):
-            xb = torch.as_tensor(X[q:q + self.max_batch], device=self.device)
-            xb = xb.unsqueeze(0).expand(self.members, -1, -1).contiguous()
+            xb = torch.as_tensor(np.ascontiguousarray(X[:, q:q + self.max_batch]), device=self.device)
             outs.append(self.forward_raw(xb))
         y = torch.cat(outs, dim=1).cpu().numpy().astype(np.float64)
         y = y * self.y_std + self.y_mean

@@ -111,3 +111,32 @@ def test_adam_step_and_training_progress(torch):
     last = E.gradients_raw(xd, td).cpu().numpy()
     assert np.all(last < 0.1 * first), (first, last)
     E.close()
+
+
+def test_surrogate_gain_over_fdtd_alone(torch):
+    """What the trained network adds to the batched FDTD: trained on the batched
+    FDTD's spectra of designs 0-4095, on 96 held-out couplers the pipeline
+    (ensemble answers where its spread is <= 1e-3, batched FDTD elsewhere) returns
+    every design faster than the batched FDTD alone, the answered designs within a
+    median RMS S-parameter error of 1e-3, and the fallback designs exactly as the
+    FDTD computes them.  (bench.py --workload surrogate runs the 256-design
+    held-out set and the 8192-query inference batch.)"""
+    from prismo_gb300 import surrogate as Su
+    from prismo_gb300 import sweep as S
+
+    train = [S.coupler_design(s) for s in range(4096)]
+    test = [S.coupler_design(s) for s in range(10000, 10096)]
+    Str = np.concatenate([S.batched_sweep(train[q:q + 1024]).S for q in range(0, 4096, 1024)])
+    ref = S.batched_sweep(test)  # the method without the network
+    E = Su.Ensemble(max_batch=1024)
+    E.fit(train, Str, epochs=Su.EPOCHS)
+    res = Su.run_pipeline(E, test)
+    err = Su.s_error(res.S, ref.S)
+    acc = res.accepted
+    print(f"accepted {acc.sum()}/{len(test)}, answered err median {np.median(err[acc]):.2e} "
+          f"max {err[acc].max():.2e}; pipeline {res.seconds:.2f} s vs FDTD {ref.seconds:.2f} s")
+    assert acc.sum() >= 5
+    assert np.all(err[~acc] == 0.0)
+    assert np.median(err[acc]) <= 1e-3
+    assert res.seconds < ref.seconds
+    E.close()

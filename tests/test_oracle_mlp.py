@@ -81,3 +81,10 @@ def test_surrogate_representation_roundtrip():
         assert abs(dist[1] - L.path) < 1e-12
     x = Su.inputs(designs)
     assert x.shape == (6, 3) and np.all(np.abs(x) <= 1)
+    # per-member random Fourier embedding: deterministic, member-specific
+    B = Su.rff_matrices()
+    e = Su.embed(x, B)
+    assert e.shape == (Su.MEMBERS, 6, Su.DIMS[0])
+    np.testing.assert_array_equal(e[:, :, :3], np.broadcast_to(x, (Su.MEMBERS, 6, 3)))
+    np.testing.assert_array_equal(Su.embed(x, Su.rff_matrices()), e)
+    assert not np.allclose(e[0, :, 3:], e[1, :, 3:])
