@@ -26,6 +26,7 @@ namespace pc {
 struct FusedMaps {
     CUtensorMap e[3];
     CUtensorMap h[3];
+    CUtensorMap cb[3];  // Cb of the E update, staged with the fields
 };
 
 namespace {
@@ -46,8 +47,9 @@ struct FusedGeom {
     static constexpr int align128(int b) { return (b + 127) / 128 * 128; }
     static constexpr int E_BOX = align128(EW * EH * (int)sizeof(T));
     static constexpr int H_BOX = align128(HW * HH * (int)sizeof(T));
-    static constexpr int STAGE = 3 * (E_BOX + H_BOX);
-    static constexpr uint32_t TX_BYTES = 3u * (EW * EH + HW * HH) * sizeof(T);
+    static constexpr int CB_BOX = align128(TZ * TY * (int)sizeof(T));  // Cb: k in [k0, k0+TZ), j in [j0, j0+TY)
+    static constexpr int STAGE = 3 * (E_BOX + H_BOX + CB_BOX);
+    static constexpr uint32_t TX_BYTES = 3u * (EW * EH + HW * HH + TZ * TY) * sizeof(T);
     static constexpr int HN_PLANE = 3 * HH * NW;  // elements of one H^{n+1/2} plane (3 comps)
     static constexpr int NHALO = (TZ + 1) + TY;   // halo H points per plane
 };
@@ -128,6 +130,9 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
 #pragma unroll
         for (int c = 0; c < 3; ++c)
             tma_load_3d(st + 3 * G::E_BOX + c * G::H_BOX, &maps.h[c], k0, j0, pl, &bars[s]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            tma_load_3d(st + 3 * (G::E_BOX + G::H_BOX) + c * G::CB_BOX, &maps.cb[c], k0, j0, pl, &bars[s]);
     };
     int issued = L < S ? L : S;
     if (helper && lane == 0)
@@ -239,20 +244,6 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
     // (the +1 halo row/column of H counts: E at the tile edge reads it)
     const bool yz_slab = CPML && (j0 < t || j0 + TY >= ny - t || k0 < t || k0 + TZ >= nz - t);
     auto x_slab = [&](int pl) { return CPML && pl >= 0 && pl < nx && (pl < t || pl >= nx - t); };
-    // L2 prefetch of the Cb values plane pl's E update will read: their loads are
-    // issued only one phase ahead of their use.  Variant without CPML code only:
-    // in the CPML variant the extra addressing spills registers, and prefetching
-    // the psi entries the same way measured slower.
-    auto prefetch_plane = [&](int pl) {
-        if (CPML || helper || pl < ib || pl >= ie) return;  // (the CPML variant has no registers to spare)
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            if (!pin[r]) continue;
-            const int64_t o = og(pl, r);
-#pragma unroll
-            for (int c = 0; c < 3; ++c) prefetch_l2(a.cb[c] + o);
-        }
-    };
 
     // ---- H^{n+1/2} at one point --------------------------------------------
     auto h_compute = [&](const T* E0, const T* E1, const T* E2, const T* Ep1, const T* Ep2, const T* H0,
@@ -317,12 +308,9 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
         for (int r = 0; r < 2; ++r) fetch(pt_at(ib, r), true, pfH[r]);
     }
     T chk = T(0);  // running sum of E^{n+1}: non-finite iff some value was
-    constexpr int PF_AHEAD = 4;
-    for (int pl = ib; pl < ib + PF_AHEAD; ++pl) prefetch_plane(pl);
     for (; n < L; ++n) {
         const int p = ib - 1 + n;  // plane whose H^{n+1/2} is computed now
         const int q = p - 1;       // plane whose E^{n+1} is computed now
-        prefetch_plane(p + PF_AHEAD);
         const bool slabH = yz_slab || x_slab(p);
         const bool slabE = yz_slab || x_slab(q);
         const unsigned char* stc = stages + sn * G::STAGE;
@@ -342,16 +330,8 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
         const T* Np0 = sHn + hp * G::HN_PLANE;
         const T* Np1 = Np0 + G::HH * NW;
         const T* Np2 = Np1 + G::HH * NW;
-        // prefetch Cb(q) for the E update while the H phase runs
-        T cb[2][3];
-        if (!helper && n >= 2) {
-#pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                const int64_t o = og(q, r);
-#pragma unroll
-                for (int c = 0; c < 3; ++c) cb[r][c] = pin[r] ? __ldg(a.cb[c] + o) : T(0);
-            }
-        }
+        // Cb(q) of the E update: staged by TMA with plane q's fields
+        const T* Cq = reinterpret_cast<const T*>(stp + 3 * (G::E_BOX + G::H_BOX));
         // x-slab coefficients of planes p and q (uniform)
         T xbH = T(1), xaH = T(0), xkH = T(1), xbE = T(1), xaE = T(0), xkE = T(1);
         if (CPML) {
@@ -436,9 +416,11 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
                         ca1 = a.ca[1][o];
                         ca2 = a.ca[2][o];
                     }
-                    if (ux) ex = ca0 * ex + cb[r][0] * (d2 - d4);
-                    if (uy) ey = ca1 * ey + cb[r][1] * (d5 - d0);
-                    if (uz) ez = ca2 * ez + cb[r][2] * (d1 - d3);
+                    const int cbo = (warp + NWC * r) * TZ + lane;
+                    const T cb0 = Cq[cbo], cb1 = Cq[G::CB_BOX / sizeof(T) + cbo], cb2 = Cq[2 * (G::CB_BOX / sizeof(T)) + cbo];
+                    if (ux) ex = ca0 * ex + cb0 * (d2 - d4);
+                    if (uy) ey = ca1 * ey + cb1 * (d5 - d0);
+                    if (uz) ez = ca2 * ez + cb2 * (d1 - d3);
                     a.Eout[0][o] = ex;
                     a.Eout[1][o] = ey;
                     a.Eout[2][o] = ez;
@@ -503,6 +485,7 @@ int make_map(CUtensorMap* m, const void* base, const pc_grid_desc& g, int bw, in
 
 struct FusedState {
     const void* key_f[2][6];
+    const void* key_cb[3];
     FusedMaps maps[2];  // per input set
     bool ready = false;
     int4* d_items = nullptr;  // work items of the current chunking: plain ones, then cpml ones
@@ -566,8 +549,9 @@ int launch_variant(cudaStream_t s, const FieldArgs<T>& a, const CpmlArgs<T>& p, 
                    const int4* items, int n_items) {
     auto kern = fused3<T, TY, TZ, S, CPML, HCOEF, CA>;
     static bool attr = false;
-    if (!attr) {
-        PC_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    if (!attr) {  // the largest size any launch asks for (CPML table for PC_MAX_CPML)
+        const int smem_max = fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * PC_MAX_CPML * (int)sizeof(T);
+        PC_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
         attr = true;
     }
     if (n_items <= 0) return PC_OK;
@@ -585,7 +569,8 @@ int choose_chunk(const pc_grid_desc& g, int smem) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     if (sms <= 0) sms = 152;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * PC_MAX_CPML * (int)sizeof(T));
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
     if (per_sm <= 0) per_sm = 1;
@@ -612,24 +597,28 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
     FusedState* st = state_of(c);
     bool same = st->ready;
     for (int q = 0; q < 6 && same; ++q) same = st->key_f[0][q] == c->F[0][q] && st->key_f[1][q] == c->F[1][q];
+    for (int q = 0; q < 3 && same; ++q) same = st->key_cb[q] == c->cb[q];
     if (!same) {
         for (int set = 0; set < 2; ++set)
             for (int q = 0; q < 3; ++q) {
                 int rc = make_map(&st->maps[set].e[q], c->F[set][q], g, G::EW, G::EH);
                 if (!rc) rc = make_map(&st->maps[set].h[q], c->F[set][3 + q], g, G::HW, G::HH);
+                if (!rc) rc = make_map(&st->maps[set].cb[q], c->cb[q], g, TZ, TY);
                 if (rc) return rc;
             }
         for (int q = 0; q < 6; ++q) {
             st->key_f[0][q] = c->F[0][q];
             st->key_f[1][q] = c->F[1][q];
         }
+        for (int q = 0; q < 3; ++q) st->key_cb[q] = c->cb[q];
         st->ready = true;
     }
     const int in = c->cur, out = c->cur ^ 1;
     FieldArgs<T> a = make_field_args<T>(c, in, out);
     CpmlArgs<T> p = make_cpml_args<T>(c, in, out);
     if (p.t > 0 && p.total >= ((int64_t)1 << 31)) return launch_split_step(c, s);  // 32-bit psi offsets
-    const int smem = fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * PC_MAX_CPML * (int)sizeof(T);
+    // dynamic shared memory: the stage ring, H^{n+1/2} planes and this grid's CPML table
+    const int smem = fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * std::max(p.t, 1) * (int)sizeof(T);
     const bool cp = p.t > 0, hc = a.da[0] != nullptr, ca = a.ca[0] != nullptr;
     const FusedMaps& m = st->maps[in];
     if (c->fused_cx <= 0) c->fused_cx = choose_chunk<T, TY, TZ, S>(g, smem);
@@ -727,7 +716,7 @@ int4* g_noalloc_ptr[128];
 template <typename T>
 int noalloc_run(const pc_grid_desc& g, void* const set0[6], void* const set1[6], int cur, const void* const cb[3],
                 int nsteps, cudaStream_t s, int4* scratch) {
-    constexpr int TY = 16, TZ = 32, S = (sizeof(T) == 4) ? 5 : 3;
+    constexpr int TY = 16, TZ = 32, S = (sizeof(T) == 4) ? 4 : 3;
     using G = FusedGeom<T, TY, TZ>;
     auto kern = fused3<T, TY, TZ, S, false, false, false>;
     const int smem = fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * PC_MAX_CPML * (int)sizeof(T);
@@ -755,6 +744,7 @@ int noalloc_run(const pc_grid_desc& g, void* const set0[6], void* const set1[6],
         for (int q = 0; q < 3; ++q) {
             int rc = make_map(&maps[set].e[q], F[q], g, G::EW, G::EH);
             if (!rc) rc = make_map(&maps[set].h[q], F[3 + q], g, G::HW, G::HH);
+            if (!rc) rc = make_map(&maps[set].cb[q], cb[q], g, TZ, TY);
             if (rc) return rc;
         }
     }
@@ -837,7 +827,7 @@ namespace {
 int launch_fused_step(pc_ctx* c, cudaStream_t s) {
     if (c->g.ndim != 3) return launch_split_step(c, s);
     if (c->g.precision == 8) return fused_t<double, 16, 32, 3>(c, s);
-    return fused_t<float, 16, 32, 5>(c, s);
+    return fused_t<float, 16, 32, 4>(c, s);
 }
 
 void destroy_fused_state(pc_ctx* c) {
