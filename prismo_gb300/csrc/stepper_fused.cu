@@ -153,19 +153,13 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
             b = T(1), aa = T(0), kk = T(1);
         }
     };
-    auto ld = [&](int o) -> T {
-        if ((unsigned)o >= (unsigned)tot) {  // range check: flag and skip
-            atomicOr(pm.status, PC_STATUS_BOUNDS);
-            return T(0);
-        }
-        return __ldg(pm.psi_in + o);
-    };
+    // psi accesses: range-checked once per work item (psi_ok, below) instead of per
+    // access; a thread whose offsets could leave [0, tot) flags PC_STATUS_BOUNDS and
+    // skips its psi traffic
+    bool psi_ok = true;
+    auto ld = [&](int o) -> T { return psi_ok ? __ldg(pm.psi_in + o) : T(0); };
     auto st = [&](int o, T v) {
-        if ((unsigned)o >= (unsigned)tot) {
-            atomicOr(pm.status, PC_STATUS_BOUNDS);
-            return;
-        }
-        pm.psi_out[o] = v;
+        if (psi_ok) pm.psi_out[o] = v;
     };
     // point state for plane pl of a point (j, k) with per-point constants
     // (syc, szc: slab indices; oyc/ozc: plane-independent parts of the offsets)
@@ -234,6 +228,24 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
         poxc[r] = (int)pm.axis_base[0] + pj[r] * P32 + pk[r];
         poyc[r] = (int)pm.axis_base[1] + (psy[r] >= 0 ? psy[r] : 0) * P32 + pk[r];
         pozc[r] = (int)pm.axis_base[2] + pj[r] * t2 + (psz[r] >= 0 ? psz[r] : 0);
+    }
+    if (CPML) {
+        // every offset a point can form over this item's planes: x-slab entries at any
+        // slab index, y/z-slab entries up to the last plane, plus the largest slot
+        const int64_t sxm = max(max(xA_H, xB_H), max(xA_E, xB_E));
+        const int64_t sym = max(max(yA_H, yB_H), max(yA_E, yB_E));
+        const int64_t szm = max(max(zA_H, zB_H), max(zA_E, zB_E));
+        const int64_t phi = min(ie, nx - 1);
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            if (!pin[r]) continue;
+            const int64_t lo_x = poxc[r], hi_x = (int64_t)poxc[r] + (int64_t)(t2 - 1) * ny * P32 + sxm;
+            bool ok = lo_x >= 0 && hi_x < tot;
+            if (psy[r] >= 0) ok = ok && poyc[r] >= 0 && (int64_t)poyc[r] + phi * t2 * P32 + sym < tot;
+            if (psz[r] >= 0) ok = ok && pozc[r] >= 0 && (int64_t)pozc[r] + phi * ny * t2 + szm < tot;
+            psi_ok = psi_ok && ok;
+        }
+        if (!psi_ok) atomicOr(pm.status, PC_STATUS_BOUNDS);
     }
     const int k = k0 + lane;  // consumers' own k
     auto pt_at = [&](int pl, int r) {
