@@ -172,9 +172,14 @@ int pc_status(pc_ctx* ctx, uint32_t* flags, void* stream);
 /* Number of this library's kernels launched since the context was created. */
 int64_t pc_launch_count(const pc_ctx* ctx);
 
-/* Tuning knobs (0 = automatic choice).  PC_TUNE_FUSED_CHUNK: planes along x
- * streamed by one CTA of the fused 3D schedule. */
+/* Tuning knobs.  PC_TUNE_FUSED_CHUNK: planes along x streamed by one CTA of the
+ * fused 3D schedule (0 = automatic choice).  PC_TUNE_GRAPH_STEPS: pc_step replays
+ * its time loop from a CUDA graph of this many steps (a multiple of 16; 0 = one
+ * launch sequence per step), captured on first use after an eager step and
+ * re-captured after any call that changes what a step launches.  Steps with a
+ * TFSF source or with pc_profile enabled always run eagerly.  Default 64. */
 #define PC_TUNE_FUSED_CHUNK 1
+#define PC_TUNE_GRAPH_STEPS 2
 int pc_set_tuning(pc_ctx* ctx, int32_t key, int64_t value);
 int64_t pc_get_tuning(const pc_ctx* ctx, int32_t key);
 

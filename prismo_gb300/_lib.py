@@ -32,6 +32,7 @@ PC_SCHED_SPLIT = 1
 PC_SCHED_FUSED = 2
 
 PC_TUNE_FUSED_CHUNK = 1
+PC_TUNE_GRAPH_STEPS = 2
 
 
 class GridDesc(C.Structure):

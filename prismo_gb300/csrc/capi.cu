@@ -120,6 +120,10 @@ int pc_create(const pc_grid_desc* desc, pc_ctx** out) {
     if (c->g.mode == PC_MODE_LEGACY || c->g.ndim == 2) c->g.sched = PC_SCHED_SPLIT;
     c->da_s = 1.0;
     c->db_s = 0.0;
+    c->gen = 1;
+    c->warm_gen = 0;
+    c->graph_steps = 64;
+    c->graph_gen[0] = c->graph_gen[1] = 0;
     if (cudaMalloc(&c->d_status, 2 * sizeof(uint32_t)) != cudaSuccess) {
         delete c;
         return PC_ERR_CUDA;
@@ -148,11 +152,16 @@ void pc_destroy(pc_ctx* c) {
     cudaFree(c->tfsf.d_h1);
     cudaFree(c->d_status);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
+    for (int q = 0; q < 2; ++q)
+        if (c->graph[q]) cudaGraphExecDestroy(c->graph[q]);
+    if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+    cudaFree(c->d_amps_g);
     destroy_fused_state(c);
     delete c;
 }
 
 int pc_set_fields(pc_ctx* c, void* const set0[6], void* const set1[6]) {
+    if (c) ++c->gen;  // captured time loops are stale
     if (!c || !set0) return PC_ERR_INVALID;
     for (int q = 0; q < 6; ++q) {
         if (!set0[q]) return PC_ERR_INVALID;
@@ -185,6 +194,7 @@ int pc_build_coefficients(pc_ctx* c, const double* eps, const double* mu, const 
 
 int pc_set_coefficients(pc_ctx* c, const void* const ca[3], const void* const cb[3],
                         const void* const da[3], const void* const db[3], double da_s, double db_s) {
+    if (c) ++c->gen;  // captured time loops are stale
     if (!c || !cb) return PC_ERR_INVALID;
     for (int q = 0; q < 3; ++q) {
         if (!cb[q]) return PC_ERR_INVALID;
@@ -207,6 +217,7 @@ size_t pc_cpml_psi_elems(const pc_grid_desc* d, int32_t t) {
 
 int pc_set_cpml(pc_ctx* c, int32_t t, const double* const b[3], const double* const a[3],
                 const double* const kappa[3], void* psi0, void* psi1) {
+    if (c) ++c->gen;  // captured time loops are stale
     if (!c) return PC_ERR_INVALID;
     if (t <= 0) {
         c->cpml_t = 0;
@@ -274,6 +285,7 @@ int pc_set_cpml(pc_ctx* c, int32_t t, const double* const b[3], const double* co
 }
 
 int pc_add_source(pc_ctx* c, int32_t comp, const int64_t* offsets, const double* weights, int32_t n) {
+    if (c) ++c->gen;  // captured time loops are stale
     if (!c || comp < 0 || comp > 5 || n <= 0 || !offsets) return PC_ERR_INVALID;
     if ((int)c->sources.size() >= PC_MAX_SOURCES) return PC_ERR_INVALID;
     const int64_t lim = (int64_t)c->g.nx * c->g.ny * c->g.pitch;
@@ -298,6 +310,99 @@ int pc_add_source(pc_ctx* c, int32_t comp, const int64_t* offsets, const double*
     c->sources.push_back(d);
     return (int)c->sources.size() - 1;
 }
+
+namespace pc {
+namespace {
+
+// One leap-frog step n of a pc_step call: stencil, sources (amplitude row n of
+// c->d_amps), DFT sampling.  tamp: host TFSF amplitude of the step (or null).
+int one_step(pc_ctx* c, int n, const double* tamp, cudaStream_t s) {
+    int rc;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (c->prof_on) {
+        if (c->prof_used + 2 > c->prof_ev.size()) {
+            for (int q = 0; q < 2; ++q) {
+                cudaEvent_t e;
+                PC_CUDA_CHECK(cudaEventCreate(&e));
+                c->prof_ev.push_back(e);
+            }
+        }
+        ev0 = c->prof_ev[c->prof_used];
+        ev1 = c->prof_ev[c->prof_used + 1];
+        c->prof_used += 2;
+        PC_CUDA_CHECK(cudaEventRecord(ev0, s));
+    }
+    if (c->g.mode == PC_MODE_LEGACY)
+        rc = launch_legacy_step(c, s);
+    else if (c->g.sched == PC_SCHED_FUSED && c->ade_n == 0 && !c->tfsf.on)
+        rc = launch_fused_step(c, s);
+    else
+        rc = launch_split_step(c, s, tamp);
+    if (rc) return rc;
+    if (ev1) PC_CUDA_CHECK(cudaEventRecord(ev1, s));
+    rc = launch_sources(c, n, s);
+    if (rc) return rc;
+    if (!c->dfts.empty()) {
+        rc = dft_after_step(c, s);
+        if (rc) return rc;
+    }
+    return PC_OK;
+}
+
+// The graph of G steps for the current set (captured on first use).  Sources read
+// their amplitude rows from c->d_amps_g, which each replay refills.
+int ensure_step_graph(pc_ctx* c, int G, size_t ns) {
+    const int q = c->cur;
+    if (c->graph[q] && c->graph_gen[q] == c->gen && c->graph_G[q] == G) return PC_OK;
+    if (c->graph[q]) {
+        cudaGraphExecDestroy(c->graph[q]);
+        c->graph[q] = nullptr;
+    }
+    if (!c->cap_stream) PC_CUDA_CHECK(cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
+    const size_t need = (size_t)G * ns;
+    if (need > c->amps_g_cap) {
+        cudaFree(c->d_amps_g);
+        c->d_amps_g = nullptr;
+        c->amps_g_cap = 0;
+        PC_CUDA_CHECK(cudaMalloc(&c->d_amps_g, std::max<size_t>(need, 1) * sizeof(double)));
+        c->amps_g_cap = need;
+    }
+    const int cur0 = c->cur;
+    const int64_t launches0 = c->launches;
+    double* amps0 = c->d_amps;
+    std::vector<int> rows0;
+    for (auto& m : c->dfts) rows0.push_back(m.rows);
+    c->d_amps = c->d_amps_g;
+    cudaGraph_t gr = nullptr;
+    PC_CUDA_CHECK(cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
+    int rc = PC_OK;
+    for (int n = 0; n < G && !rc; ++n) rc = one_step(c, n, nullptr, c->cap_stream);
+    const cudaError_t e = cudaStreamEndCapture(c->cap_stream, &gr);
+    const int64_t nodes = c->launches - launches0;
+    c->d_amps = amps0;
+    c->cur = cur0;
+    c->launches = launches0;
+    for (size_t i = 0; i < c->dfts.size(); ++i) c->dfts[i].rows = rows0[i];
+    if (rc || e != cudaSuccess) {
+        if (gr) cudaGraphDestroy(gr);
+        cudaGetLastError();
+        return rc ? rc : PC_ERR_CUDA;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&c->graph[q], gr, 0);
+    cudaGraphDestroy(gr);
+    if (ei != cudaSuccess) {
+        c->graph[q] = nullptr;
+        cudaGetLastError();
+        return PC_ERR_CUDA;
+    }
+    c->graph_gen[q] = c->gen;
+    c->graph_G[q] = G;
+    c->graph_nodes[q] = nodes;
+    return PC_OK;
+}
+
+}  // namespace
+}  // namespace pc
 
 int pc_step(pc_ctx* c, int32_t nsteps, const double* amps, void* stream) {
     if (!c || nsteps < 0) return PC_ERR_INVALID;
@@ -326,43 +431,40 @@ int pc_step(pc_ctx* c, int32_t nsteps, const double* amps, void* stream) {
         if (need) PC_CUDA_CHECK(cudaMemcpyAsync(c->d_amps, src_tab, need * sizeof(double), cudaMemcpyHostToDevice, s));
         if (ncol != ns) PC_CUDA_CHECK(cudaStreamSynchronize(s));  // amps_host is reused by the next call
     }
-    for (int n = 0; n < nsteps; ++n) {
-        int rc;
-        cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-        if (c->prof_on) {
-            if (c->prof_used + 2 > c->prof_ev.size()) {
-                for (int q = 0; q < 2; ++q) {
-                    cudaEvent_t e;
-                    PC_CUDA_CHECK(cudaEventCreate(&e));
-                    c->prof_ev.push_back(e);
-                }
+    // the time loop replays a captured graph of G steps where it can: no per-step
+    // host data (TFSF amplitudes, profiling events), DFT rings at a batch boundary,
+    // and the launch setup done by an earlier eager step of the same configuration
+    const int G = c->graph_steps;
+    const bool graphable = G > 0 && G % 16 == 0 && !c->prof_on && !c->tfsf.on;
+    int n = 0;
+    while (n < nsteps) {
+        bool rows0 = true;
+        for (auto& m : c->dfts) rows0 = rows0 && m.rows == 0;
+        if (graphable && c->warm_gen == c->gen && rows0 && nsteps - n >= G) {
+            const int rc = ensure_step_graph(c, G, ns);
+            if (rc == PC_OK) {
+                if (ns)
+                    PC_CUDA_CHECK(cudaMemcpyAsync(c->d_amps_g, c->d_amps + (size_t)n * ns, (size_t)G * ns * sizeof(double),
+                                                  cudaMemcpyDeviceToDevice, s));
+                PC_CUDA_CHECK(cudaGraphLaunch(c->graph[c->cur], s));
+                c->launches += c->graph_nodes[c->cur];
+                n += G;
+                continue;
             }
-            ev0 = c->prof_ev[c->prof_used];
-            ev1 = c->prof_ev[c->prof_used + 1];
-            c->prof_used += 2;
-            PC_CUDA_CHECK(cudaEventRecord(ev0, s));
+            c->graph_steps = 0;  // capture is not possible here: stay eager
         }
         const double* tamp = c->tfsf.on ? &amps[(size_t)n * ncol + ns] : nullptr;
-        if (c->g.mode == PC_MODE_LEGACY)
-            rc = launch_legacy_step(c, s);
-        else if (c->g.sched == PC_SCHED_FUSED && c->ade_n == 0 && !c->tfsf.on)
-            rc = launch_fused_step(c, s);
-        else
-            rc = launch_split_step(c, s, tamp);
+        const int rc = one_step(c, n, tamp, s);
         if (rc) return rc;
-        if (ev1) PC_CUDA_CHECK(cudaEventRecord(ev1, s));
-        rc = launch_sources(c, n, s);
-        if (rc) return rc;
-        if (!c->dfts.empty()) {
-            rc = dft_after_step(c, s);
-            if (rc) return rc;
-        }
+        c->warm_gen = c->gen;
+        ++n;
     }
     return PC_OK;
 }
 
 int pc_add_dft(pc_ctx* c, int32_t comp, const int64_t* offsets, int32_t npts, const double* omega, int32_t nf,
                double dt, double t0, void* d_acc) {
+    if (c) ++c->gen;  // captured time loops are stale
     if (!c || comp < 0 || comp > 5) return PC_ERR_INVALID;
     DftMonitor m{};
     const int rc = dft_monitor_init(m, comp, offsets, npts, omega, nf, dt, t0, d_acc,
@@ -373,6 +475,7 @@ int pc_add_dft(pc_ctx* c, int32_t comp, const int64_t* offsets, int32_t npts, co
 }
 
 int pc_set_ade(pc_ctx* c, int32_t n, const pc_ade_region* regs, double eps0) {
+    if (c) ++c->gen;  // captured time loops are stale
     if (!c || n < 0 || n > PC_MAX_ADE_REGIONS || (n > 0 && !regs) || !(eps0 > 0)) return PC_ERR_INVALID;
     if (n > 0 && c->g.mode == PC_MODE_LEGACY) return PC_ERR_INVALID;  // no ADE coupling in the reference
     const double dt = c->g.dt;
@@ -412,6 +515,7 @@ int pc_set_ade(pc_ctx* c, int32_t n, const pc_ade_region* regs, double eps0) {
 
 int pc_set_tfsf(pc_ctx* c, int32_t k0, int32_t direction, int32_t polarization, int32_t m0, int32_t aux_len,
                 double eps_b, double eps0) {
+    if (c) ++c->gen;  // captured time loops are stale
     if (!c || c->g.ndim != 3 || c->g.mode != PC_MODE_CORRECTED) return PC_ERR_INVALID;
     if (direction != 1 && direction != -1) return PC_ERR_INVALID;
     if (polarization != 0 && polarization != 1) return PC_ERR_INVALID;
@@ -452,11 +556,16 @@ int pc_status(pc_ctx* c, uint32_t* flags, void* stream) {
 int64_t pc_launch_count(const pc_ctx* c) { return c ? c->launches : -1; }
 
 int pc_set_tuning(pc_ctx* c, int32_t key, int64_t value) {
+    if (c) ++c->gen;  // captured time loops are stale
     if (!c) return PC_ERR_INVALID;
     switch (key) {
         case PC_TUNE_FUSED_CHUNK:
             if (value < 0 || value > c->g.nx) return PC_ERR_INVALID;
             c->fused_cx = (int)value;
+            return PC_OK;
+        case PC_TUNE_GRAPH_STEPS:
+            if (value < 0 || value % 16 != 0 || value > (1 << 20)) return PC_ERR_INVALID;
+            c->graph_steps = (int)value;
             return PC_OK;
         default:
             return PC_ERR_INVALID;
@@ -466,6 +575,7 @@ int pc_set_tuning(pc_ctx* c, int32_t key, int64_t value) {
 int64_t pc_get_tuning(const pc_ctx* c, int32_t key) {
     if (!c) return PC_ERR_INVALID;
     if (key == PC_TUNE_FUSED_CHUNK) return c->fused_cx;
+    if (key == PC_TUNE_GRAPH_STEPS) return c->graph_steps;
     return PC_ERR_INVALID;
 }
 

@@ -151,6 +151,18 @@ struct pc_ctx {
     uint32_t* d_status;
     uint32_t* d_legacy_flags;
     int64_t launches;
+    // captured time loop (pc_step): graphs of graph_steps steps, one per starting set,
+    // valid while `gen` (bumped by every call that changes what a step launches) holds
+    int64_t gen;
+    int64_t warm_gen;  // gen of the last eager step: first-launch setup has run
+    int graph_steps;
+    cudaStream_t cap_stream;
+    cudaGraphExec_t graph[2];
+    int64_t graph_gen[2];
+    int graph_G[2];
+    int64_t graph_nodes[2];
+    double* d_amps_g;  // amplitude rows of the chunk a graph replay runs
+    size_t amps_g_cap;
 };
 
 // ---- launchers (host functions, defined in the .cu files) -------------------

@@ -429,6 +429,10 @@ class FDTDEngine:
     def chunk(self) -> int:
         return int(self.lib.pc_get_tuning(self.ctx, _lib.PC_TUNE_FUSED_CHUNK))
 
+    def set_graph_steps(self, n: int):
+        """Steps per captured time-loop graph (a multiple of 16; 0 = eager steps)."""
+        _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_GRAPH_STEPS, int(n)), "pc_set_tuning")
+
     def launch_count(self) -> int:
         return int(self.lib.pc_launch_count(self.ctx))
 

@@ -240,3 +240,47 @@ def test_fused_plain_and_cpml_item_classes(torch, chunk):
             tol = 1e-12 if prec == "fp64" else 1e-5
             assert rel_l2(out[c], o.F[c]) <= tol, (prec, c, rel_l2(out[c], o.F[c]))
         eng.close()
+
+
+@pytest.mark.parametrize("is2d", [True, False])
+def test_captured_time_loop_matches_eager_steps(torch, is2d):
+    """pc_step replays graphs of 64 steps (sources read their rows from a refilled
+    table; DFT rings flush inside the graph): bit-identical to per-step launches,
+    also across a change of configuration between calls (a source added later)."""
+    from prismo_gb300.pml import PMLParams
+
+    if is2d:
+        g = O.OracleGrid.from_total(96, 70, 1, 20e-9, 8)
+        idx = g.component_indices("Ez", 30, 31, 20, 50, 0, 1)
+        idx2 = g.component_indices("Ez", 60, 61, 30, 31, 0, 1)
+        comp = "Ez"
+    else:
+        g = O.OracleGrid.from_total(40, 36, 48, 20e-9, 6)
+        idx = g.component_indices("Ez", 20, 21, 18, 19, 24, 25)
+        idx2 = g.component_indices("Ex", 12, 13, 10, 11, 30, 31)
+        comp = "Ez"
+    dt = g.suggest_dt(0.5)
+    rng = np.random.default_rng(4)
+    mats = {"eps_rel": rng.uniform(1.0, 4.0, size=g.dims)}
+    wf = O.gaussian_pulse(193e12, 2e-15)
+    mon = g.component_indices(comp, 10, 30, 10, 30, 0, 1) if is2d else g.component_indices(comp, 10, 30, 10, 20, 20, 21)
+    freqs = np.linspace(180e12, 200e12, 5)
+    outs = []
+    for graph_steps in (0, 64):
+        eng = make_engine(g.dims, g.spacing, dt, is2d, precision="fp32", material_arrays=mats,
+                          pml=PMLParams(thickness=6 if not is2d else 8))
+        eng.set_graph_steps(graph_steps)
+        eng.add_source(comp, eng.offsets(comp, idx), None, wf)
+        m = eng.add_dft(comp, eng.offsets(comp, mon), freqs, t0=dt)
+        t = (np.arange(300) + 1) * dt
+        eng.step(150, np.array([wf(x) for x in t[:150]])[:, None])
+        # a second source from step 150 on: the captured graph must be re-captured
+        eng.add_source("Ex" if not is2d else "Ez", eng.offsets("Ex" if not is2d else "Ez", idx2), None, wf)
+        a2 = np.stack([np.array([wf(x) for x in t[150:]]), 0.5 * np.array([wf(x) for x in t[150:]])], axis=1)
+        eng.step(150, a2)
+        assert eng.check_status() == 0
+        outs.append((read_fields(eng), eng.dft_result(m).cpu().numpy(), eng.launch_count()))
+        eng.close()
+    for c in (("Ez", "Hx", "Hy") if is2d else COMPS):
+        assert np.array_equal(outs[0][0][c], outs[1][0][c]), c
+    assert np.array_equal(outs[0][1], outs[1][1])
