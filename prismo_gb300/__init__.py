@@ -14,9 +14,11 @@ from .sources import (  # noqa: F401,E402
     ContinuousWave,
     CustomWaveform,
     ElectricDipole,
+    GaussianBeamSource,
     GaussianPulse,
     LineSource,
     MagneticDipole,
+    ModeSource,
     PlaneWaveSource,
     PointSource,
     Source,

@@ -81,6 +81,10 @@ def _identity(a):
     return a
 
 
+def _per_z0(a):  # gaussian.py:262-266: H carries a / 377
+    return a / 377.0
+
+
 class Source(ABC):
     """sources/base.py:17-150 (same constructor and region semantics)."""
 
@@ -121,7 +125,7 @@ class Source(ABC):
         """Host path for fields that are not bound to a device engine."""
         if not self.enabled:
             return
-        a = self.waveform(time)
+        a = self.amplitude(time)
         for comp, idx, w, fn in self.injections():
             f = fields[comp]
             f[idx] += fn(a) if w is None else (w * fn(a))
@@ -232,6 +236,117 @@ class LineSource(Source):
         return [(self.component, idx, w, _identity)]
 
 
+class GaussianBeamSource(Source):
+    """sources/gaussian.py:18-298: on the source region, E += a(t) exp(-r^2/w0^2) and
+    H += a(t) exp(-r^2/w0^2) / 377 with r the transverse distance of each region
+    point from the beam centre (the reference's profile of _calculate_beam_profile,
+    160-268, over the region's index ranges; each component's index set takes the
+    profile values in C order, as ``field[indices] += values.flat`` does)."""
+
+    _MAP = PlaneWaveSource._MAP
+
+    def __init__(self, center, size, direction: str, polarization: str, frequency: float, beam_waist: float,
+                 pulse: bool = True, pulse_width: Optional[float] = None, amplitude: float = 1.0,
+                 phase: float = 0.0, name: Optional[str] = None, enabled: bool = True):
+        super().__init__(center=center, size=size, name=name, enabled=enabled)
+        if direction.lower() == polarization.lower():
+            raise ValueError(f"Polarization ({polarization}) must be perpendicular to propagation direction "
+                             f"({direction})")
+        if (direction.lower(), polarization.lower()) not in self._MAP:
+            raise ValueError(f"Invalid direction ({direction}) and polarization ({polarization}) combination")
+        self.direction = direction
+        self.polarization = polarization
+        self.frequency = frequency
+        self.beam_waist = beam_waist
+        if pulse:
+            if pulse_width is None:
+                raise ValueError("pulse_width must be provided for pulsed sources")
+            self.waveform = GaussianPulse(frequency, pulse_width, amplitude, phase)
+        else:
+            self.waveform = ContinuousWave(frequency, amplitude, phase)
+
+    def beam_profile(self) -> np.ndarray:
+        """exp(-r^2 / w0^2) on the region's transverse index grid (no time factor)."""
+        g = self._grid
+        x0, x1, y0, y1, z0, z1 = self._compute_source_region()
+        is3d = getattr(g, "is_3d", len(g.dimensions) == 3 and g.dimensions[2] > 1)
+        if not is3d and z0 == z1:
+            z1 = z0 + 1
+        d = self.direction.lower()
+        if d == "x":
+            ys, zs = np.meshgrid(np.arange(y0, y1), np.arange(z0, z1), indexing="ij")
+            r2 = (g.index_to_coord(1, ys) - self.center[1]) ** 2
+            if is3d:
+                r2 = r2 + (g.index_to_coord(2, zs) - self.center[2]) ** 2
+        elif d == "y":
+            xs, zs = np.meshgrid(np.arange(x0, x1), np.arange(z0, z1), indexing="ij")
+            r2 = (g.index_to_coord(0, xs) - self.center[0]) ** 2
+            if is3d:
+                r2 = r2 + (g.index_to_coord(2, zs) - self.center[2]) ** 2
+        else:
+            xs, ys = np.meshgrid(np.arange(x0, x1), np.arange(y0, y1), indexing="ij")
+            r2 = (g.index_to_coord(0, xs) - self.center[0]) ** 2 + (g.index_to_coord(1, ys) - self.center[1]) ** 2
+        return np.exp(-r2 / self.beam_waist**2)
+
+    def injections(self):
+        e, h = self._MAP[(self.direction.lower(), self.polarization.lower())]
+        prof = self.beam_profile().ravel()
+        out = []
+        for comp, fn in ((e, _identity), (h, _per_z0)):
+            idx = self._source_region[comp]
+            shape = tuple(np.asarray(i).size for i in idx)
+            n = int(np.prod(shape))
+            if prof.size != n:
+                raise ValueError(f"beam profile has {prof.size} values for {n} {comp} points of the region")
+            out.append((comp, idx, prof.reshape(shape), fn))
+        return out
+
+
+class ModeSource(Source):
+    """sources/mode.py:19-361: a waveguide mode injected on a plane.  The mode's
+    transverse field profiles (real parts, already sampled on the source plane's
+    points of each component: ``profiles = {component: array}``) are added with
+    the amplitude A w(t) cos(phase - omega t) (update_fields, 198-253: the real part
+    of A w(t) exp(i(phase - omega t))); the normal H component takes the
+    propagation sign (+x/-x, ...)."""
+
+    def __init__(self, center, size, profiles: dict, direction: str, waveform: Waveform, frequency: float,
+                 amplitude: float = 1.0, phase: float = 0.0, name: Optional[str] = None, enabled: bool = True):
+        super().__init__(center=center, size=size, name=name, enabled=enabled)
+        if direction[0] not in "+-" or direction[-1].lower() not in "xyz":
+            raise ValueError("direction must be one of +x, -x, +y, -y, +z, -z")
+        self.direction = direction
+        self.sign = +1 if direction[0] == "+" else -1
+        self.axis = direction[-1].lower()
+        self.profiles = {c: np.asarray(v, dtype=np.float64) for c, v in profiles.items()}
+        self.waveform = waveform
+        self.frequency = frequency
+        self.amplitude_scale = amplitude
+        self.phase = phase
+
+    def _normal_h(self) -> str:
+        return {"x": "Hx", "y": "Hy", "z": "Hz"}[self.axis]
+
+    def injections(self):
+        out = []
+        for comp, prof in self.profiles.items():
+            idx = self._source_region[comp]
+            shape = tuple(np.asarray(i).size for i in idx)
+            if prof.size != int(np.prod(shape)):
+                raise ValueError(f"{comp} profile has {prof.size} values for {int(np.prod(shape))} points")
+            w = prof.reshape(shape) * (self.sign if comp == self._normal_h() else 1.0)
+            out.append((comp, idx, w, _identity))
+        return out
+
+    def mode_amplitude(self, t):
+        """A w(t) cos(phase - omega t) at simulation time t."""
+        omega = 2 * np.pi * self.frequency
+        return self.amplitude_scale * np.asarray(self.waveform(t)) * np.cos(self.phase - omega * np.asarray(t))
+
+    def amplitude(self, t):
+        return self.mode_amplitude(t)
+
+
 class TFSFSource(Source):
     """Plane-wave total-field/scattered-field source (sources/tfsf.py:17-411
     interface).  On the device it is a consistent TFSF plane fed by a 1D auxiliary
@@ -274,7 +389,7 @@ def amplitude_table(sources: Sequence[Source], times: np.ndarray) -> np.ndarray:
     """[len(times), n_injections] amplitudes (disabled sources contribute 0)."""
     cols = []
     for s in sources:
-        a = np.asarray(s.waveform(times), dtype=np.float64) if s.enabled else np.zeros(len(times))
+        a = np.asarray(s.amplitude(times), dtype=np.float64) if s.enabled else np.zeros(len(times))
         a = np.broadcast_to(a, (len(times),))
         for _, _, _, fn in s.injections():
             cols.append(np.broadcast_to(fn(a), (len(times),)))

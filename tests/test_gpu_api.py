@@ -145,3 +145,39 @@ def test_tfsf_through_simulation(pg):
     o.run(n)
     for c in COMPS:
         assert rel(sim.fields[c].to_numpy(), o.F[c]) <= 1e-5, c
+
+
+def test_beam_and_mode_sources_through_simulation(pg):
+    """GaussianBeamSource (E and H/377 soft sources over a beam profile) and
+    ModeSource (mode profiles times A w(t) cos(phase - omega t)) through the
+    Simulation API on the device, against the float64 oracle with the same
+    injections: fields rel L2 <= 1e-5."""
+    size = ((40 - 8 - 0.5) * 20e-9, (36 - 8 - 0.5) * 20e-9, (32 - 8 - 0.5) * 20e-9)
+    sim = pg.Simulation(size=size, resolution=1 / 20e-9, pml_layers=4, courant_factor=0.5)
+    gb = pg.GaussianBeamSource(center=(0.2e-6, 0.28e-6, 0.24e-6), size=(0.0, 0.2e-6, 0.16e-6), direction="x",
+                               polarization="z", frequency=193e12, beam_waist=0.08e-6, pulse_width=4e-15)
+    sim.add_source(gb)
+    mc, msz = (0.45e-6, 0.25e-6, 0.22e-6), (0.0, 0.12e-6, 0.1e-6)
+    probe = pg.ModeSource(mc, msz, {}, "-x", pg.GaussianPulse(193e12, 4e-15), 193e12)
+    probe.initialize(sim.grid)
+    rng = np.random.default_rng(5)
+    prof = {c: rng.standard_normal(int(np.prod([np.asarray(i).size for i in probe._source_region[c]])))
+            for c in ("Ey", "Ez", "Hx")}
+    ms = pg.ModeSource(mc, msz, prof, "-x", pg.GaussianPulse(193e12, 4e-15), 193e12, amplitude=0.7, phase=0.4)
+    sim.add_source(ms)
+    n = 120
+    sim.run(n * sim.dt * (1 - 1e-12))
+    assert sim.step_count == n
+    g = O.OracleGrid(size, 1 / 20e-9, 4)
+    o = O.OracleFDTD(g, g.suggest_dt(0.5), cpml_layers=4)
+    wf = O.gaussian_pulse(193e12, 4e-15)
+    for comp, idx, w, fn in gb.injections():
+        o.add_source(comp, idx, (lambda t, fn=fn: fn(wf(t))), weight=w)
+    om = 2 * np.pi * 193e12
+    for comp, idx, w, fn in ms.injections():
+        o.add_source(comp, idx, (lambda t: 0.7 * wf(t) * np.cos(0.4 - om * t)), weight=w)
+    o.run(n)
+    for c in COMPS:
+        assert np.abs(o.F[c]).max() > 0, c
+        assert rel(sim.fields[c].to_numpy(), o.F[c]) <= 1e-5, (c, rel(sim.fields[c].to_numpy(), o.F[c]))
+    assert sim.check() == 0

@@ -87,3 +87,44 @@ def test_materials_match_reference_coefficients(golden_dir):
     np.testing.assert_allclose(lor.permittivity(z["eps_w"]), z["eps_lorentz"], rtol=1e-13)
     np.testing.assert_allclose(DrudeMaterial(1.0, 1.37e16, 1.0e14).permittivity(z["eps_w"]), z["eps_drude"],
                                rtol=1e-13)
+
+
+def test_gaussian_beam_and_mode_sources_host_side():
+    """GaussianBeamSource (sources/gaussian.py:167-298): E weights exp(-r^2/w0^2)
+    over the region in C order, H the same with a / 377; ModeSource
+    (sources/mode.py:198-361): A w(t) cos(phase - omega t), normal H signed."""
+    from prismo_gb300.grid import YeeGrid
+    from prismo_gb300.sources import GaussianBeamSource, GaussianPulse, ModeSource, amplitude_table
+
+    g = YeeGrid.from_total((40, 30, 26), 20e-9, 4)
+    gb = GaussianBeamSource(center=(0.3e-6, 0.2e-6, 0.18e-6), size=(0.0, 0.2e-6, 0.16e-6), direction="x",
+                            polarization="z", frequency=193e12, beam_waist=0.1e-6, pulse_width=5e-15)
+    gb.initialize(g)
+    x0, x1, y0, y1, z0, z1 = gb._compute_source_region()
+    ys, zs = np.meshgrid(np.arange(y0, y1), np.arange(z0, z1), indexing="ij")
+    want = np.exp(-((g.index_to_coord(1, ys) - 0.2e-6) ** 2 + (g.index_to_coord(2, zs) - 0.18e-6) ** 2) / 1e-14)
+    inj = gb.injections()
+    assert [i[0] for i in inj] == ["Ez", "Hy"]
+    np.testing.assert_allclose(inj[0][2].ravel(), want.ravel(), rtol=1e-14)
+    np.testing.assert_allclose(inj[1][2].ravel(), want.ravel(), rtol=1e-14)
+    t = np.cumsum(np.full(20, 3e-17))
+    tab = amplitude_table([gb], t)
+    wf = O.gaussian_pulse(193e12, 5e-15)
+    np.testing.assert_array_equal(tab[:, 0], [wf(x) for x in t])
+    np.testing.assert_array_equal(tab[:, 1], [wf(x) / 377.0 for x in t])
+
+    ms_center, ms_size = (0.2e-6, 0.2e-6, 0.2e-6), (0.0, 0.1e-6, 0.1e-6)
+    probe = ModeSource(ms_center, ms_size, {}, "-x", GaussianPulse(193e12, 5e-15), 193e12)
+    probe.initialize(g)
+    shp = {c: tuple(np.asarray(i).size for i in probe._source_region[c]) for c in ("Ey", "Ez", "Hx")}
+    rng = np.random.default_rng(1)
+    prof = {c: rng.standard_normal(int(np.prod(shp[c]))) for c in shp}
+    ms = ModeSource(ms_center, ms_size, prof, "-x", GaussianPulse(193e12, 5e-15), 193e12, amplitude=2.0,
+                    phase=0.3)
+    ms.initialize(g)
+    inj = {c: w for c, _, w, _ in ms.injections()}
+    np.testing.assert_array_equal(inj["Ey"].ravel(), prof["Ey"])
+    np.testing.assert_array_equal(inj["Hx"].ravel(), -prof["Hx"])  # -x: the normal H is negated
+    a = amplitude_table([ms], t)[:, 0]
+    np.testing.assert_allclose(a, 2.0 * np.array([wf(x) for x in t]) * np.cos(0.3 - 2 * np.pi * 193e12 * t),
+                               rtol=1e-14, atol=1e-300)
