@@ -148,6 +148,13 @@ def _adapt_source(src):
         out.frequency = getattr(src, "frequency", None)
         out.waveform = src.waveform
         return out
+    if name == "GaussianBeamSource":
+        out = S.GaussianBeamSource.__new__(S.GaussianBeamSource)
+        S.Source.__init__(out, center=src.center, size=src.size, name=src.name, enabled=src.enabled)
+        out.direction, out.polarization = src.direction, src.polarization
+        out.frequency, out.beam_waist = src.frequency, src.beam_waist
+        out.waveform = src.waveform
+        return out
     return src  # unknown type: applied from the host on device arrays
 
 

@@ -117,3 +117,20 @@ def test_reference_api_on_cuda(prismo_installed):
         assert np.abs(mon.get_frequency_data("Ez", 193e12)).max() > 0
     finally:
         prismo.set_backend("numpy")
+
+
+def test_reference_gaussian_beam_is_adapted(prismo):
+    """A reference GaussianBeamSource becomes the device source with the same
+    region, profile parameters and waveform (no GPU needed)."""
+    from prismo.sources.gaussian import GaussianBeamSource as RefBeam
+
+    from prismo_gb300 import plugin
+    from prismo_gb300 import sources as S
+
+    ref = RefBeam(center=(0.2e-6, 0.2e-6, 0.2e-6), size=(0.0, 0.2e-6, 0.2e-6), direction="x", polarization="z",
+                  frequency=193e12, beam_waist=0.1e-6, pulse=True, pulse_width=4e-15)
+    out = plugin._adapt_source(ref)
+    assert isinstance(out, S.GaussianBeamSource)
+    assert (out.direction, out.polarization, out.beam_waist, out.frequency) == ("x", "z", 0.1e-6, 193e12)
+    assert out.waveform is ref.waveform
+    assert tuple(out.center) == tuple(ref.center) and tuple(out.size) == tuple(ref.size)
