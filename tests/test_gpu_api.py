@@ -151,7 +151,7 @@ def test_beam_and_mode_sources_through_simulation(pg):
     """GaussianBeamSource (E and H/377 soft sources over a beam profile) and
     ModeSource (mode profiles times A w(t) cos(phase - omega t)) through the
     Simulation API on the device, against the float64 oracle with the same
-    injections: fields rel L2 <= 1e-5."""
+    injections: each component's L2 error <= 1e-5 of its field family's norm."""
     size = ((40 - 8 - 0.5) * 20e-9, (36 - 8 - 0.5) * 20e-9, (32 - 8 - 0.5) * 20e-9)
     sim = pg.Simulation(size=size, resolution=1 / 20e-9, pml_layers=4, courant_factor=0.5)
     gb = pg.GaussianBeamSource(center=(0.2e-6, 0.28e-6, 0.24e-6), size=(0.0, 0.2e-6, 0.16e-6), direction="x",
@@ -177,7 +177,11 @@ def test_beam_and_mode_sources_through_simulation(pg):
     for comp, idx, w, fn in ms.injections():
         o.add_source(comp, idx, (lambda t: 0.7 * wf(t) * np.cos(0.4 - om * t)), weight=w)
     o.run(n)
+    # per component, relative to its family (components only excited indirectly are
+    # small, so their own float32 relative error is not the measure)
+    fam = {f: np.sqrt(sum(np.linalg.norm(o.F[c]) ** 2 for c in COMPS if c[0] == f)) for f in "EH"}
     for c in COMPS:
         assert np.abs(o.F[c]).max() > 0, c
-        assert rel(sim.fields[c].to_numpy(), o.F[c]) <= 1e-5, (c, rel(sim.fields[c].to_numpy(), o.F[c]))
+        err = np.linalg.norm(sim.fields[c].to_numpy() - o.F[c]) / fam[c[0]]
+        assert err <= 1e-5, (c, err)
     assert sim.check() == 0
