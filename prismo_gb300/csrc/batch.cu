@@ -85,13 +85,18 @@ template <int TX, int TY, int K>
 struct BShape {
     static_assert(TY % 2 == 0, "the fast path moves y-adjacent pairs");
     static constexpr int RX = TX + 2 * K, RY = TY + 2 * K, RC = RX * RY, M = (RC + BNT - 1) / BNT;
-    // two CTAs per SM (64 registers a thread) while the per-cell registers fit
+    static constexpr int MP = (RC / 2 + BNT - 1) / BNT;  // cell pairs per thread (fast path)
+    // general path: two CTAs per SM (64 registers a thread) while the per-cell
+    // registers fit; fast path: three CTAs per SM (42 registers) while its pairs fit
     static constexpr int MINB = M <= 8 ? 2 : 1;
+    static constexpr int MINB_FAST = MP <= 4 ? 3 : (MP <= 8 ? 2 : 1);
     // Ez, Hx, Hy with RY + 2 guard cells on both sides (the fast path reads
-    // neighbours of edge cells without tests), then the four CPML auxiliaries
+    // neighbours of edge cells without tests), then (general path only) the four
+    // CPML auxiliaries
     static constexpr int GUARD = RY + 2;  // even: the float2 accesses stay 8-byte aligned
     static constexpr int FS = RC + 2 * GUARD;
     static constexpr size_t SMEM = sizeof(float) * (3 * FS + 4 * RC);
+    static constexpr size_t SMEM_FAST = sizeof(float) * 3 * FS;
 };
 
 // The update formulas with explicit rounding (no contraction choices left to the
@@ -109,8 +114,11 @@ __device__ __forceinline__ float h_plus(float h, float d, float da, float db) { 
 }
 __device__ __forceinline__ float diff(float a, float b, float inv) { return __fmul_rn(__fsub_rn(a, b), inv); }
 
-template <int TX, int TY, int K>
-__global__ void __launch_bounds__(BNT, BShape<TX, TY, K>::MINB) batch2d_pass(BPass P) {
+// FAST: the kernel of the fast-path items (their own table and launch, with the
+// smaller shared-memory footprint and higher occupancy); otherwise the general items.
+template <int TX, int TY, int K, bool FAST>
+__global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BShape<TX, TY, K>::MINB)
+    batch2d_pass(BPass P) {
     using SH = BShape<TX, TY, K>;
     constexpr int RX = SH::RX, RY = SH::RY, RC = SH::RC;
     constexpr int M = SH::M;
@@ -146,7 +154,7 @@ __global__ void __launch_bounds__(BNT, BShape<TX, TY, K>::MINB) batch2d_pass(BPa
         const float* fin = P.fin + sI.f_off;
         float* fout = P.fout + sI.f_off;
         const float* cbp = P.cb + sI.c_off;
-        if ((it.w & 3) == 0) {
+        if (FAST) {
             // ---- fast path: the region lies inside the instance, clear of the CPML,
             // the source column and the port lines: every cell updates every component
             // (edge cells read guard or wrapped neighbours; their results fall outside
@@ -383,12 +391,18 @@ __global__ void batch_advance(long long* step, int n) {
 
 struct Variant {
     int tx, ty, k, k1;  // tile, steps per pass, index of the K=1 sibling
-    const void* fn;
-    size_t smem;
+    const void* fn[2];  // [0]: fast-path items, [1]: general items
+    size_t smem[2];
 };
 
-#define PC_BV(TX, TY, K, K1) \
-    {TX, TY, K, K1, reinterpret_cast<const void*>(&batch2d_pass<TX, TY, K>), BShape<TX, TY, K>::SMEM}
+#define PC_BV(TX, TY, K, K1)                                                                          \
+    {TX,                                                                                              \
+     TY,                                                                                              \
+     K,                                                                                               \
+     K1,                                                                                              \
+     {reinterpret_cast<const void*>(&batch2d_pass<TX, TY, K, true>),                                 \
+      reinterpret_cast<const void*>(&batch2d_pass<TX, TY, K, false>)},                                \
+     {BShape<TX, TY, K>::SMEM_FAST, BShape<TX, TY, K>::SMEM}}
 const Variant kVariants[] = {
     PC_BV(32, 64, 1, 0),  PC_BV(32, 64, 2, 0),  PC_BV(32, 64, 4, 0),  PC_BV(32, 64, 8, 0),
     PC_BV(16, 128, 1, 4), PC_BV(16, 128, 2, 4), PC_BV(16, 128, 4, 4), PC_BV(64, 64, 1, 7),
@@ -429,10 +443,11 @@ struct pc_batch {
     int variant = 1;
     int graph_steps = 80;
     int item_variant = -1;
-    int4* d_items = nullptr;
+    int4* d_items = nullptr;  // fast-path items, then general items
     int nitems = 0;
+    int nfast = 0;
     int items_cap = 0;
-    int grid[kNumVariants] = {};
+    int grid[kNumVariants][2] = {};
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int graph_key[2][2] = {{-1, -1}, {-1, -1}};  // (variant, graph_steps) the graph was captured for
@@ -484,9 +499,18 @@ int build_items(pc_batch* b, int v) {
     if (b->d_items) drop_graphs(b);  // captured graphs hold the previous table
     std::vector<int> ord(items.size());
     std::iota(ord.begin(), ord.end(), 0);
-    std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) { return cost[a] > cost[c]; });
+    // fast-path items first, then the general ones; each class longest first
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) {
+        const bool fa = (items[a].w & 3) == 0, fc = (items[c].w & 3) == 0;
+        if (fa != fc) return fa;
+        return cost[a] > cost[c];
+    });
     std::vector<int4> sorted(items.size());
-    for (size_t q = 0; q < ord.size(); ++q) sorted[q] = items[ord[q]];
+    int nfast = 0;
+    for (size_t q = 0; q < ord.size(); ++q) {
+        sorted[q] = items[ord[q]];
+        nfast += (sorted[q].w & 3) == 0 ? 1 : 0;
+    }
     if ((int)sorted.size() > b->items_cap) {
         cudaFree(b->d_items);
         b->d_items = nullptr;
@@ -496,21 +520,23 @@ int build_items(pc_batch* b, int v) {
     }
     PC_CUDA_CHECK(cudaMemcpy(b->d_items, sorted.data(), sorted.size() * sizeof(int4), cudaMemcpyHostToDevice));
     b->nitems = (int)sorted.size();
+    b->nfast = nfast;
     b->item_variant = v;
     return PC_OK;
 }
 
-int grid_for(pc_batch* b, int v) {
-    if (b->grid[v] > 0) return b->grid[v];
+int grid_for(pc_batch* b, int v, int path) {
+    if (b->grid[v][path] > 0) return b->grid[v][path];
     int dev = 0, nsm = 0, occ = 0;
+    const Variant& V = kVariants[v];
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaFuncSetAttribute(kVariants[v].fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)kVariants[v].smem) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kVariants[v].fn, BNT, kVariants[v].smem) != cudaSuccess)
+        cudaFuncSetAttribute(V.fn[path], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)V.smem[path]) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, V.fn[path], BNT, V.smem[path]) != cudaSuccess)
         return -1;
-    b->grid[v] = std::max(1, nsm * std::max(1, occ));
-    return b->grid[v];
+    b->grid[v][path] = std::max(1, nsm * std::max(1, occ));
+    return b->grid[v][path];
 }
 
 // A pass reads the current set and writes the other one, so a dry pass (live = 0)
@@ -544,14 +570,24 @@ BPass make_pass(pc_batch* b, int s_off, int row0, bool live) {
     return P;
 }
 
-int launch_pass(pc_batch* b, int v, const BPass& P, cudaStream_t s) {
-    const int g = grid_for(b, v);
-    if (g <= 0) return PC_ERR_CUDA;
-    const int grid = std::min(g, std::max(1, P.nitems));
-    void* args[] = {const_cast<BPass*>(&P)};
-    PC_CUDA_CHECK(cudaLaunchKernel(kVariants[v].fn, dim3(grid), dim3(BNT), args, kVariants[v].smem, s));
-    ++b->launches;
-    return PC_OK;
+// One pass = the fast-path items' kernel, then the general items' kernel; returns
+// the number of kernels launched (or a negative error).
+int launch_pass(pc_batch* b, int v, const BPass& P0, cudaStream_t s) {
+    int launched = 0;
+    for (int path = 0; path < 2; ++path) {
+        BPass P = P0;
+        P.items = P0.items + (path == 0 ? 0 : b->nfast);
+        P.nitems = path == 0 ? b->nfast : P0.nitems - b->nfast;
+        if (P.nitems <= 0) continue;
+        const int g = grid_for(b, v, path);
+        if (g <= 0) return PC_ERR_CUDA;
+        const int grid = std::min(g, P.nitems);
+        void* args[] = {&P};
+        PC_CUDA_CHECK(cudaLaunchKernel(kVariants[v].fn[path], dim3(grid), dim3(BNT), args, kVariants[v].smem[path], s));
+        ++b->launches;
+        ++launched;
+    }
+    return launched;
 }
 
 // One chunk of eager passes of variant v covering `steps` steps starting at ring row
@@ -568,8 +604,8 @@ int run_passes(pc_batch* b, int v, int steps, cudaStream_t s, int* nodes) {
         // the K=1 sibling reuses the table of v (same tiles; halo flags computed for K >= 1)
         BPass P = make_pass(b, done, b->dft_rows, true);
         int rc = launch_pass(b, vv, P, s);
-        if (rc) return rc;
-        ++*nodes;
+        if (rc < 0) return rc;
+        *nodes += rc;
         b->cur ^= 1;
         done += k;
         if (b->have_dft) {
@@ -598,7 +634,9 @@ int ensure_graph(pc_batch* b) {
         b->graph[q] = nullptr;
     }
     if (!b->cap_stream) PC_CUDA_CHECK(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
-    if (grid_for(b, b->variant) <= 0 || grid_for(b, kVariants[b->variant].k1) <= 0) return PC_ERR_CUDA;
+    for (int path = 0; path < 2; ++path)
+        if (grid_for(b, b->variant, path) <= 0 || grid_for(b, kVariants[b->variant].k1, path) <= 0)
+            return PC_ERR_CUDA;
     const int cur0 = b->cur, rows0 = b->dft_rows;
     const long long launches0 = b->launches;
     int nodes = 0;
@@ -843,11 +881,11 @@ int pc_batch_autotune(pc_batch* b, int32_t passes, float* ms_per_step, void* str
         if (rc) return rc;
         BPass P = make_pass(b, 0, 0, false);
         rc = launch_pass(b, v, P, s);  // warm-up
-        if (rc) return rc;
+        if (rc < 0) return rc;
         PC_CUDA_CHECK(cudaEventRecord(e0, s));
         for (int q = 0; q < passes; ++q) {
             rc = launch_pass(b, v, P, s);
-            if (rc) return rc;
+            if (rc < 0) return rc;
         }
         PC_CUDA_CHECK(cudaEventRecord(e1, s));
         PC_CUDA_CHECK(cudaEventSynchronize(e1));
