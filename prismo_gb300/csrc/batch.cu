@@ -1,26 +1,30 @@
 // Batched 2D sweep engine: many uneven 2D TE simulations (Ez, Hx, Hy: the
 // reference's "TE mode", core/solver.py:311-456 with the corrected stencil)
-// advanced together by one persistent kernel per pass.
+// advanced together by persistent kernels.
 //
 // The reference runs a parameter sweep one design after another
 // (optimization/sweep.py:41-195, each design a full Simulation.run).  Here every
 // design of a sweep is an *instance* whose Ez/Hx/Hy live in shared device buffers
-// at per-instance offsets; a host-built work table lists (instance, tile) items,
-// LPT-sorted, and a persistent grid of CTAs walks it.
+// at per-instance offsets; a host-built work table lists (instance, tile) items
+// and persistent grids of CTAs walk it.
 //
 // One pass advances every instance by K steps (temporal blocking): a CTA loads
 // its tile plus a K-cell halo of Ez, Hx, Hy into shared memory, runs K leap-frog
 // steps there (the valid region shrinks by one cell per side per step), and
-// writes the tile interior to the other field set (ping-pong).  Per-cell state
-// that no neighbour reads -- Cb(Ez) and the four CPML auxiliaries -- stays in
-// registers for the whole pass.  The soft mode-profile line source is added in
-// the E phase (sources/point.py:62-73 semantics, amplitude at t_{n+1}) and the
-// port DFT lines are sampled into the shared DFT ring in the same phase.  The
-// time loop is captured once as a CUDA graph of G steps and replayed; a device
-// step counter drives the amplitude table.
+// writes the tile interior to the other field set (ping-pong).  Items fall in two
+// classes, each with its own kernel: tiles whose region lies inside the instance
+// and clear of the CPML, the source column and the port lines take a branch-free
+// path (no per-cell tests, y-adjacent cell pairs as float2, three shared arrays);
+// the others keep per-cell validity flags and Cb in registers and the four CPML
+// auxiliaries in shared memory, add the soft mode-profile line source in the E
+// phase (sources/point.py:62-73 semantics, amplitude at t_{n+1}) and sample the
+// port DFT lines into the shared DFT ring.  The time loop is captured once as a
+// CUDA graph of G steps and replayed; a device step counter drives the amplitude
+// table.
 //
-// Arithmetic per point is the single-simulation 2D stepper's (stepper_split.cu
-// split_h2 / split_e2 Ez family): same operations in the same order.
+// Arithmetic per point is that of the single-simulation 2D stepper (stepper_split.cu
+// split_h2 / split_e2 Ez family), with every rounding explicit so that both
+// classes and every tile shape give the same bits.
 #include <algorithm>
 #include <cstring>
 #include <numeric>
