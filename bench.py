@@ -631,16 +631,23 @@ def run_surrogate(args, cpu):
     _, spread_q, _ = E.predict(q)
     t_inf = time.perf_counter() - t0
     xd = torch.as_tensor(E._features(Su.inputs(q)), device="cuda")
-    for _ in range(3):
-        E.forward_raw(xd)
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record()
-    for _ in range(20):
-        E.forward_raw(xd)
-    ev1.record()
-    torch.cuda.synchronize()
-    fwd_ms = ev0.elapsed_time(ev1) / 20
+
+    def forward_ms():
+        for _ in range(3):
+            E.forward_raw(xd)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(20):
+            E.forward_raw(xd)
+        ev1.record()
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / 20
+
+    E.set_tensor_path(False)
+    fwd_ms_mma = forward_ms()
+    E.set_tensor_path(True)
+    fwd_ms = forward_ms()
     dims = E.dims
     flops = E.members * 8192 * 2 * (32 * dims[1] + dims[1] * dims[2] + dims[2] * dims[3] + dims[3] * dims[4])
     r_fdtd = len(test) / ref.seconds
@@ -664,6 +671,7 @@ def run_surrogate(args, cpu):
           inference={"queries": 8192, "seconds": t_inf, "designs_per_s": 8192 / t_inf,
                      "accept_fraction": float(np.mean(spread_q <= Su.THRESHOLD)),
                      "device_forward_ms": fwd_ms, "device_tflops": flops / (fwd_ms * 1e-3) / 1e12,
+                     "device_forward_ms_mma_sync": fwd_ms_mma,
                      "pipeline_designs_per_s_8192": dps_8192,
                      "pipeline_vs_serial_8192": dps_8192 / ser.designs_per_s},
           e2e={"value": res.designs_per_s, "unit": "designs/s", "h2d_bytes_per_step": len(test) * 12,

@@ -157,6 +157,8 @@ SIGNATURES = {
     "pc_mlp_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.c_float, C.c_float,
                                     C.c_float, C.c_void_p, C.c_void_p]),
     "pc_mlp_launch_count": (C.c_int64, [C.c_void_p]),
+    "pc_mlp_set_tensor_path": (C.c_int, [C.c_void_p, C.c_int32]),
+    "pc_mlp_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p]),
     "pc_mlp_destroy": (None, [C.c_void_p]),
 }
 

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "pc_internal.cuh"
+#include "tcgen05.cuh"
 
 namespace pc {
 namespace {
@@ -181,6 +182,168 @@ __global__ void __launch_bounds__(128) mlp_gemm(GemmP p) {
         }
 }
 
+// The forward products on the 5th-generation tensor cores: a 128-row x 256-column
+// output tile per CTA (4 warps), accumulated in tensor memory by tcgen05.mma
+// (kind::f16: bf16 x bf16 -> f32, M 128, N 256, K 16 per instruction) issued by one
+// thread.  K runs in chunks of 32 through a 3-stage ring: every thread copies its
+// 16-byte pieces with cp.async into 8-row x 16-byte core matrices (no swizzle,
+// K-major), and a stage is refilled once the tcgen05.commit of the MMAs that read
+// it has arrived on its mbarrier.  SPLIT: the hi and lo activation tiles go through
+// two MMAs into the same accumulator.  Epilogue: tcgen05.ld (warp w owns lanes
+// 32w..32w+31, one output row per thread) in 32-column slices; the transposed
+// bf16 copy is written straight from that layout (consecutive rows per warp), the
+// row-major outputs after a per-warp transpose through shared memory so that each
+// warp store covers 32 consecutive columns of one row.
+constexpr int TC_M = 128, TC_N = 256, TC_K = 32, TC_NST = 3;
+constexpr uint32_t TC_LBO = 128;                // core matrices adjacent along K
+constexpr uint32_t TC_SBO = (TC_K / 8) * 128;   // core matrices adjacent along M / N
+constexpr int TC_A_BYTES = TC_M * TC_K * 2;     // 8 KB
+constexpr int TC_B_BYTES = TC_N * TC_K * 2;     // 16 KB
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
+
+template <bool SPLIT>
+__host__ __device__ constexpr int tc_stage_bytes() {
+    return (SPLIT ? 2 : 1) * TC_A_BYTES + TC_B_BYTES;
+}
+template <bool SPLIT>
+__host__ __device__ constexpr int tc_smem_bytes() {
+    return 1024 + TC_NST * tc_stage_bytes<SPLIT>();
+}
+static_assert(4 * 32 * 33 * 4 <= TC_NST * tc_stage_bytes<false>(), "epilogue scratch fits the stages");
+
+// byte offset of element (row, k) of a K-major chunk in the core-matrix layout
+__device__ __forceinline__ int cm_off(int row, int k) {
+    return (row >> 3) * TC_SBO + (k >> 3) * TC_LBO + (row & 7) * 16 + (k & 7) * 2;
+}
+
+template <int MODE, bool SPLIT>
+__global__ void __launch_bounds__(128) mlp_gemm_tc(GemmP p, unsigned* status) {
+    static_assert(MODE == EP_HIDDEN || MODE == EP_OUT, "forward epilogues only");
+    extern __shared__ __align__(1024) unsigned char tsm[];
+    unsigned char* base = tsm + ((1024u - (smem_u32(tsm) & 1023u)) & 1023u);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base);            // [TC_NST]
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(base + 64);     // allocated tensor-memory address
+    unsigned char* stages = base + 1024;
+    const int z = blockIdx.z;
+    const int m0 = blockIdx.y * TC_M, n0 = blockIdx.x * TC_N;
+    const bf16* A = p.A + z * p.sA;
+    const bf16* A2 = SPLIT ? p.A2 + z * p.sA : nullptr;
+    const bf16* B = p.B + z * p.sB;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nk = p.K / TC_K;
+
+    if (warp == 0) tmem_alloc(tslot, TC_N);
+    if (tid == 0) {
+        for (int i = 0; i < TC_NST; ++i) mbar_init(&bars[i], 1);
+        fence_mbar_init();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    constexpr uint32_t idesc = idesc_bf16_f32(TC_M, TC_N);
+
+    // chunk kc -> stage kc % TC_NST; kc >= nk commits an empty group
+    auto load = [&](int kc) {
+        if (kc < nk) {
+            unsigned char* sA = stages + (kc % TC_NST) * tc_stage_bytes<SPLIT>();
+            unsigned char* sB = sA + (SPLIT ? 2 : 1) * TC_A_BYTES;
+            const int k0 = kc * TC_K;
+            for (int q = tid; q < TC_M * 4; q += 128) {
+                const int row = q >> 2, kq = (q & 3) * 8;
+                const bool valid = m0 + row < p.M;
+                const int64_t src = (int64_t)(valid ? m0 + row : 0) * p.lda + k0 + kq;
+                cp_async16(sA + cm_off(row, kq), A + src, valid);
+                if (SPLIT) cp_async16(sA + TC_A_BYTES + cm_off(row, kq), A2 + src, valid);
+            }
+            for (int q = tid; q < TC_N * 4; q += 128) {
+                const int row = q >> 2, kq = (q & 3) * 8;
+                cp_async16(sB + cm_off(row, kq), B + (int64_t)(n0 + row) * p.ldb + k0 + kq, true);
+            }
+        }
+        cp_async_commit();
+    };
+
+    for (int kc = 0; kc < TC_NST - 1; ++kc) load(kc);
+    bool ok = true;
+    for (int kc = 0; kc < nk; ++kc) {
+        cp_async_wait<TC_NST - 2>();  // this thread's pieces of chunk kc have landed
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            unsigned char* sA = stages + (kc % TC_NST) * tc_stage_bytes<SPLIT>();
+            unsigned char* sB = sA + (SPLIT ? 2 : 1) * TC_A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < TC_K / 16; ++kk) {
+                const uint64_t bd = smem_desc(sB + kk * 2 * TC_LBO, TC_LBO, TC_SBO);
+                tc_mma_bf16(tmem, smem_desc(sA + kk * 2 * TC_LBO, TC_LBO, TC_SBO), bd, idesc, kc > 0 || kk > 0);
+                if (SPLIT)
+                    tc_mma_bf16(tmem, smem_desc(sA + TC_A_BYTES + kk * 2 * TC_LBO, TC_LBO, TC_SBO), bd, idesc, true);
+            }
+            tc_commit(&bars[kc % TC_NST]);
+        }
+        // refill the stage of chunk kc - 1 with chunk kc + TC_NST - 1 once its MMAs are done
+        const int nx = kc + TC_NST - 1;
+        if (nx < nk && kc >= 1 && ok)
+            ok = mbar_wait_bounded(&bars[(kc - 1) % TC_NST], (uint32_t)(((kc - 1) / TC_NST) & 1), TC_WAIT_LIMIT);
+        load(ok ? nx : nk);
+    }
+    // the last chunk's commit covers every MMA issued before it
+    const int lb = (nk - 1) % TC_NST;
+    const uint32_t lpar = (uint32_t)(((nk - 1) / TC_NST) & 1);
+    if (ok) ok = mbar_wait_bounded(&bars[lb], lpar, TC_WAIT_LIMIT);
+    ok = __syncthreads_and(ok);  // uniform: the epilogue's tcgen05.ld and __syncwarp need whole warps
+    if (!ok) {
+        if (tid == 0) atomicOr(status, PC_STATUS_TIMEOUT);
+        // in-flight MMAs still read shared memory and write tensor memory: wait for them
+        // once more (bounded) before tensor memory is released
+        mbar_wait_bounded(&bars[lb], lpar, TC_WAIT_LIMIT);
+    }
+    cp_async_wait<0>();
+    tc_fence_after();
+    if (ok) {
+        float* scr = reinterpret_cast<float*>(stages) + warp * (32 * 33);  // this warp's 32 x 33 slice
+        const int mw = m0 + warp * 32;
+        const float* bias = p.bias + z * p.sBias;
+#pragma unroll 1
+        for (int c = 0; c < TC_N; c += 32) {
+            float v[32];
+            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+            const int nb = n0 + c;
+            if (MODE == EP_HIDDEN && mw + lane < p.M) {
+                bf16* ot = p.outT + z * p.sOT + mw + lane;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const float x = v[j] + bias[nb + j];
+                    ot[(int64_t)(nb + j) * p.ldt] = __float2bfloat16_rn(x * sigm(x));
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 32; ++j) scr[lane * 33 + j] = v[j];
+            __syncwarp();
+            const float bn = bias[nb + lane];
+            const int rows = min(32, p.M - mw);
+#pragma unroll 4
+            for (int r = 0; r < rows; ++r) {
+                const int64_t m = mw + r;
+                const float x = scr[r * 33 + lane] + bn;
+                p.outF[z * p.sO + m * p.ldo + nb + lane] = x;
+                if (MODE == EP_HIDDEN) {
+                    const float av = x * sigm(x);
+                    const bf16 a = __float2bfloat16_rn(av);
+                    p.outB[z * p.sOB + m * p.ldb2 + nb + lane] = a;
+                    p.outB2[z * p.sOB + m * p.ldb2 + nb + lane] = __float2bfloat16_rn(av - __bfloat162float(a));
+                }
+            }
+            __syncwarp();
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, TC_N);
+}
+
 // x [z][B][din] float -> bf16 pair [z][B][kp] (hi, lo) and hi [z][kp][B] (member stride
 // Bmax * kp), zero padded
 __global__ void mlp_pack(const float* __restrict__ x, int din, int kp, int B, int Bmax, bf16* __restrict__ xb,
@@ -316,6 +479,8 @@ struct pc_mlp {
     bf16* grT[4] = {};
     float* d_loss = nullptr;
     long long t = 0;     // Adam steps taken
+    int tc = 1;          // forward products on tcgen05 (1) or mma.sync (0)
+    unsigned* d_status = nullptr;
     long long launches = 0;
     std::vector<void*> allocs;
 };
@@ -358,6 +523,25 @@ int gemm(pc_mlp* n, GemmP p, cudaStream_t s) {
     return PC_OK;
 }
 
+// forward products (split activations): tcgen05 when the shape fits its tiles
+template <int MODE>
+int gemm_fwd(pc_mlp* n, GemmP p, cudaStream_t s) {
+    if (!n->tc || p.N % TC_N != 0 || p.K % TC_K != 0) return gemm<MODE, true>(n, p, s);
+    // at least 110 KB of shared memory: at most two CTAs per SM, so that their 2 x 256
+    // tensor-memory columns fit the SM's 512 and no allocation ever waits
+    constexpr int smem = tc_smem_bytes<true>() > 110 * 1024 ? tc_smem_bytes<true>() : 110 * 1024;
+    static bool attr = false;
+    if (!attr) {
+        PC_CUDA_CHECK(cudaFuncSetAttribute(mlp_gemm_tc<MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr = true;
+    }
+    dim3 grd(p.N / TC_N, (p.M + TC_M - 1) / TC_M, n->members);
+    mlp_gemm_tc<MODE, true><<<grd, 128, smem, s>>>(p, n->d_status);
+    ++n->launches;
+    PC_CUDA_CHECK(cudaGetLastError());
+    return PC_OK;
+}
+
 // forward of every member on x [members][B][din]; leaves z, activations, y
 int forward(pc_mlp* n, const float* x, int B, cudaStream_t s) {
     const int M = n->members;
@@ -390,12 +574,12 @@ int forward(pc_mlp* n, const float* x, int B, cudaStream_t s) {
             p.outT = n->actT[l];
             p.ldt = B;
             p.sOT = (int64_t)n->max_batch * n->nn[l];
-            rc = gemm<EP_HIDDEN, true>(n, p, s);
+            rc = gemm_fwd<EP_HIDDEN>(n, p, s);
         } else {
             p.outF = n->y;
             p.ldo = n->nn[3];
             p.sO = (int64_t)n->max_batch * n->nn[3];
-            rc = gemm<EP_OUT, true>(n, p, s);
+            rc = gemm_fwd<EP_OUT>(n, p, s);
         }
         if (rc) return rc;
     }
@@ -489,7 +673,8 @@ int pc_mlp_create(int32_t members, int32_t max_batch, const int32_t dims[5], pc_
     int rc = mlp_alloc(n, &n->w, Mb * off) || mlp_alloc(n, &n->g, Mb * off) || mlp_alloc(n, &n->m, Mb * off) ||
              mlp_alloc(n, &n->v, Mb * off) || mlp_alloc(n, &n->xb, Mb * B * 32) || mlp_alloc(n, &n->xb2, Mb * B * 32) ||
              mlp_alloc(n, &n->xt, Mb * B * 32) ||
-             mlp_alloc(n, &n->y, Mb * B * n->nn[3]) || mlp_alloc(n, &n->d_loss, Mb);
+             mlp_alloc(n, &n->y, Mb * B * n->nn[3]) || mlp_alloc(n, &n->d_loss, Mb) ||
+             mlp_alloc(n, &n->d_status, 1);
     for (int l = 0; l < 4 && !rc; ++l) {
         rc = mlp_alloc(n, &n->wb[l], Mb * n->nn[l] * n->kp[l]) || mlp_alloc(n, &n->wt[l], Mb * n->nn[l] * n->kp[l]) ||
              mlp_alloc(n, &n->gr[l], Mb * B * n->nn[l]) || mlp_alloc(n, &n->grT[l], Mb * B * n->nn[l]);
@@ -587,6 +772,20 @@ int pc_mlp_train_step(pc_mlp* n, const float* d_x, const float* d_t, int32_t bat
 }
 
 int64_t pc_mlp_launch_count(const pc_mlp* n) { return n ? n->launches : PC_ERR_INVALID; }
+
+int pc_mlp_set_tensor_path(pc_mlp* n, int32_t tcgen05) {
+    if (!n || (tcgen05 != 0 && tcgen05 != 1)) return PC_ERR_INVALID;
+    n->tc = tcgen05;
+    return PC_OK;
+}
+
+int pc_mlp_status(pc_mlp* n, uint32_t* flags, void* stream) {
+    if (!n || !flags) return PC_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    PC_CUDA_CHECK(cudaMemcpyAsync(flags, n->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    PC_CUDA_CHECK(cudaStreamSynchronize(s));
+    return PC_OK;
+}
 
 void pc_mlp_destroy(pc_mlp* n) {
     if (!n) return;

@@ -204,6 +204,15 @@ class Ensemble:
     def launches(self) -> int:
         return int(self.lib.pc_mlp_launch_count(self.h))
 
+    def set_tensor_path(self, tcgen05: bool):
+        """Forward products on tcgen05 (True) or mma.sync (False)."""
+        _lib.check(self.lib.pc_mlp_set_tensor_path(self.h, 1 if tcgen05 else 0), "pc_mlp_set_tensor_path")
+
+    def status(self) -> int:
+        v = C.c_uint32(0)
+        _lib.check(self.lib.pc_mlp_status(self.h, C.byref(v), self._stream()), "pc_mlp_status")
+        return int(v.value)
+
     def _stream(self):
         return self.torch.cuda.current_stream(self.device).cuda_stream
 

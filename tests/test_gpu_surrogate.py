@@ -140,3 +140,21 @@ def test_surrogate_gain_over_fdtd_alone(torch):
     assert np.median(err[acc]) <= 1e-3
     assert res.seconds < ref.seconds
     E.close()
+
+
+def test_tcgen05_forward_matches_mma_sync(torch):
+    """The forward products on tcgen05 (tensor-memory accumulator) equal the
+    mma.sync products up to float32 summation order (rel 1e-5), including a
+    partial 128-row tile; the oracle check of the gradients holds on this path."""
+    E, p, x, t = make(torch, members=2, batch=320, seed=9)
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda")
+    E.set_tensor_path(False)
+    y0 = E.forward_raw(xd).cpu().numpy()
+    E.set_tensor_path(True)
+    y1 = E.forward_raw(xd).cpu().numpy()
+    assert E.status() == 0
+    assert rel(y1, y0) <= 1e-5, rel(y1, y0)
+    for m in range(E.members):
+        want, _ = mlp64.forward(p[m], x[m], DIMS)
+        assert rel(y1[m], want) <= 1e-2
+    E.close()
