@@ -183,22 +183,25 @@ __global__ void __launch_bounds__(128) mlp_gemm(GemmP p) {
 }
 
 // The forward products on the 5th-generation tensor cores: a 128-row x 256-column
-// output tile per CTA (4 warps), accumulated in tensor memory by tcgen05.mma
+// output tile per CTA (8 warps), accumulated in tensor memory by tcgen05.mma
 // (kind::f16: bf16 x bf16 -> f32, M 128, N 256, K 16 per instruction) issued by one
 // thread.  K runs in chunks of 32 through a 3-stage ring: every thread copies its
 // 16-byte pieces with cp.async into 8-row x 16-byte core matrices (no swizzle,
 // K-major), and a stage is refilled once the tcgen05.commit of the MMAs that read
 // it has arrived on its mbarrier.  SPLIT: the hi and lo activation tiles go through
-// two MMAs into the same accumulator.  Epilogue: tcgen05.ld (warp w owns lanes
-// 32w..32w+31, one output row per thread) in 32-column slices; the transposed
-// bf16 copy is written straight from that layout (consecutive rows per warp), the
-// row-major outputs after a per-warp transpose through shared memory so that each
-// warp store covers 32 consecutive columns of one row.
-constexpr int TC_M = 128, TC_N = 256, TC_K = 32, TC_NST = 3;
+// two MMAs into the same accumulator.  Epilogue: warps w and w + 4 share tensor-
+// memory lanes 32(w%4)..+31 (one output row per thread) and split the columns;
+// per 32-column slice, tcgen05.ld, bias (a lane shuffle) and SiLU once per
+// element, the transposed bf16 copy written straight from that layout (each warp
+// store covers 32 consecutive rows), the row-major outputs after a per-warp
+// transpose through shared memory (row stride 36 floats: conflict-free 16-byte
+// accesses) as 16-byte / 8-byte stores of 4 columns per lane.
+constexpr int TC_M = 128, TC_N = 256, TC_K = 32, TC_NST = 3, TC_THREADS = 256;
 constexpr uint32_t TC_LBO = 128;                // core matrices adjacent along K
 constexpr uint32_t TC_SBO = (TC_K / 8) * 128;   // core matrices adjacent along M / N
 constexpr int TC_A_BYTES = TC_M * TC_K * 2;     // 8 KB
 constexpr int TC_B_BYTES = TC_N * TC_K * 2;     // 16 KB
+constexpr int TC_SCR = 32 * 36;                 // floats of one transpose slice
 constexpr uint32_t TC_WAIT_LIMIT = 1u << 24;
 
 template <bool SPLIT>
@@ -209,16 +212,24 @@ template <bool SPLIT>
 __host__ __device__ constexpr int tc_smem_bytes() {
     return 1024 + TC_NST * tc_stage_bytes<SPLIT>();
 }
-static_assert(4 * 32 * 33 * 4 <= TC_NST * tc_stage_bytes<false>(), "epilogue scratch fits the stages");
 
 // byte offset of element (row, k) of a K-major chunk in the core-matrix layout
 __device__ __forceinline__ int cm_off(int row, int k) {
     return (row >> 3) * TC_SBO + (k >> 3) * TC_LBO + (row & 7) * 16 + (k & 7) * 2;
 }
 
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    const uint32_t a = __bfloat16_as_ushort(__float2bfloat16_rn(lo));
+    const uint32_t b = __bfloat16_as_ushort(__float2bfloat16_rn(hi));
+    return a | (b << 16);
+}
+
 template <int MODE, bool SPLIT>
-__global__ void __launch_bounds__(128) mlp_gemm_tc(GemmP p, unsigned* status) {
+__global__ void __launch_bounds__(TC_THREADS) mlp_gemm_tc(GemmP p, unsigned* status) {
     static_assert(MODE == EP_HIDDEN || MODE == EP_OUT, "forward epilogues only");
+    constexpr int NSCR = MODE == EP_HIDDEN ? 2 : 1;  // pre-activation (+ activation) slices
+    static_assert(TC_THREADS / 32 * NSCR * TC_SCR * 4 <= TC_NST * tc_stage_bytes<SPLIT>(),
+                  "epilogue scratch fits the stages");
     extern __shared__ __align__(1024) unsigned char tsm[];
     unsigned char* base = tsm + ((1024u - (smem_u32(tsm) & 1023u)) & 1023u);
     uint64_t* bars = reinterpret_cast<uint64_t*>(base);            // [TC_NST]
@@ -249,14 +260,14 @@ __global__ void __launch_bounds__(128) mlp_gemm_tc(GemmP p, unsigned* status) {
             unsigned char* sA = stages + (kc % TC_NST) * tc_stage_bytes<SPLIT>();
             unsigned char* sB = sA + (SPLIT ? 2 : 1) * TC_A_BYTES;
             const int k0 = kc * TC_K;
-            for (int q = tid; q < TC_M * 4; q += 128) {
+            for (int q = tid; q < TC_M * 4; q += TC_THREADS) {
                 const int row = q >> 2, kq = (q & 3) * 8;
                 const bool valid = m0 + row < p.M;
                 const int64_t src = (int64_t)(valid ? m0 + row : 0) * p.lda + k0 + kq;
                 cp_async16(sA + cm_off(row, kq), A + src, valid);
                 if (SPLIT) cp_async16(sA + TC_A_BYTES + cm_off(row, kq), A2 + src, valid);
             }
-            for (int q = tid; q < TC_N * 4; q += 128) {
+            for (int q = tid; q < TC_N * 4; q += TC_THREADS) {
                 const int row = q >> 2, kq = (q & 3) * 8;
                 cp_async16(sB + cm_off(row, kq), B + (int64_t)(n0 + row) * p.ldb + k0 + kq, true);
             }
@@ -303,37 +314,56 @@ __global__ void __launch_bounds__(128) mlp_gemm_tc(GemmP p, unsigned* status) {
     cp_async_wait<0>();
     tc_fence_after();
     if (ok) {
-        float* scr = reinterpret_cast<float*>(stages) + warp * (32 * 33);  // this warp's 32 x 33 slice
-        const int mw = m0 + warp * 32;
+        float* sx = reinterpret_cast<float*>(stages) + warp * NSCR * TC_SCR;  // this warp's slices
+        float* sa = sx + TC_SCR;
+        const int quarter = warp & 3, c0 = (warp >> 2) * (TC_N / 2);
+        const int mw = m0 + quarter * 32;
+        const bool rowv = mw + lane < p.M;
         const float* bias = p.bias + z * p.sBias;
+        const int rr = lane >> 3, cq = (lane & 7) * 4;  // transposed phase: row in a group of 4, column quad
 #pragma unroll 1
-        for (int c = 0; c < TC_N; c += 32) {
+        for (int c = c0; c < c0 + TC_N / 2; c += 32) {
             float v[32];
-            tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+            tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c, v);
             const int nb = n0 + c;
-            if (MODE == EP_HIDDEN && mw + lane < p.M) {
-                bf16* ot = p.outT + z * p.sOT + mw + lane;
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const float x = v[j] + bias[nb + j];
-                    ot[(int64_t)(nb + j) * p.ldt] = __float2bfloat16_rn(x * sigm(x));
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < 32; ++j) scr[lane * 33 + j] = v[j];
-            __syncwarp();
             const float bn = bias[nb + lane];
-            const int rows = min(32, p.M - mw);
-#pragma unroll 4
-            for (int r = 0; r < rows; ++r) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 4) {
+                float4 xv, av;
+                float* xp = &xv.x;
+                float* ap = &av.x;
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const float x = v[j + t] + __shfl_sync(0xffffffffu, bn, j + t);
+                    xp[t] = x;
+                    if (MODE == EP_HIDDEN) {
+                        ap[t] = x * sigm(x);
+                        if (rowv) p.outT[z * p.sOT + (int64_t)(nb + j + t) * p.ldt + mw + lane] =
+                            __float2bfloat16_rn(ap[t]);
+                    }
+                }
+                *reinterpret_cast<float4*>(&sx[lane * 36 + j]) = xv;
+                if (MODE == EP_HIDDEN) *reinterpret_cast<float4*>(&sa[lane * 36 + j]) = av;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int r0 = 0; r0 < 32; r0 += 4) {
+                const int r = r0 + rr;
                 const int64_t m = mw + r;
-                const float x = scr[r * 33 + lane] + bn;
-                p.outF[z * p.sO + m * p.ldo + nb + lane] = x;
-                if (MODE == EP_HIDDEN) {
-                    const float av = x * sigm(x);
-                    const bf16 a = __float2bfloat16_rn(av);
-                    p.outB[z * p.sOB + m * p.ldb2 + nb + lane] = a;
-                    p.outB2[z * p.sOB + m * p.ldb2 + nb + lane] = __float2bfloat16_rn(av - __bfloat162float(a));
+                if (m < p.M) {
+                    const float4 x = *reinterpret_cast<const float4*>(&sx[r * 36 + cq]);
+                    *reinterpret_cast<float4*>(&p.outF[z * p.sO + m * p.ldo + nb + cq]) = x;
+                    if (MODE == EP_HIDDEN) {
+                        const float4 a = *reinterpret_cast<const float4*>(&sa[r * 36 + cq]);
+                        const uint2 hi = make_uint2(pack_bf16x2(a.x, a.y), pack_bf16x2(a.z, a.w));
+                        const float l0 = a.x - __bfloat162float(__float2bfloat16_rn(a.x));
+                        const float l1 = a.y - __bfloat162float(__float2bfloat16_rn(a.y));
+                        const float l2 = a.z - __bfloat162float(__float2bfloat16_rn(a.z));
+                        const float l3 = a.w - __bfloat162float(__float2bfloat16_rn(a.w));
+                        const uint2 lo = make_uint2(pack_bf16x2(l0, l1), pack_bf16x2(l2, l3));
+                        *reinterpret_cast<uint2*>(&p.outB[z * p.sOB + m * p.ldb2 + nb + cq]) = hi;
+                        *reinterpret_cast<uint2*>(&p.outB2[z * p.sOB + m * p.ldb2 + nb + cq]) = lo;
+                    }
                 }
             }
             __syncwarp();
@@ -526,7 +556,10 @@ int gemm(pc_mlp* n, GemmP p, cudaStream_t s) {
 // forward products (split activations): tcgen05 when the shape fits its tiles
 template <int MODE>
 int gemm_fwd(pc_mlp* n, GemmP p, cudaStream_t s) {
-    if (!n->tc || p.N % TC_N != 0 || p.K % TC_K != 0) return gemm<MODE, true>(n, p, s);
+    // the epilogue stores 4 columns (16 bytes of float32) at a time: the output (a
+    // caller's buffer for the last layer) and its strides must keep that aligned
+    const bool aligned = ((uintptr_t)p.outF & 15) == 0 && p.ldo % 4 == 0 && p.sO % 4 == 0;
+    if (!n->tc || !aligned || p.N % TC_N != 0 || p.K % TC_K != 0) return gemm<MODE, true>(n, p, s);
     // at least 110 KB of shared memory: at most two CTAs per SM, so that their 2 x 256
     // tensor-memory columns fit the SM's 512 and no allocation ever waits
     constexpr int smem = tc_smem_bytes<true>() > 110 * 1024 ? tc_smem_bytes<true>() : 110 * 1024;
@@ -536,7 +569,7 @@ int gemm_fwd(pc_mlp* n, GemmP p, cudaStream_t s) {
         attr = true;
     }
     dim3 grd(p.N / TC_N, (p.M + TC_M - 1) / TC_M, n->members);
-    mlp_gemm_tc<MODE, true><<<grd, 128, smem, s>>>(p, n->d_status);
+    mlp_gemm_tc<MODE, true><<<grd, TC_THREADS, smem, s>>>(p, n->d_status);
     ++n->launches;
     PC_CUDA_CHECK(cudaGetLastError());
     return PC_OK;

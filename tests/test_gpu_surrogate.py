@@ -13,6 +13,7 @@ import numpy as np
 import pytest
 
 from oracle import mlp64
+from prismo_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
 
@@ -154,6 +155,11 @@ def test_tcgen05_forward_matches_mma_sync(torch):
     y1 = E.forward_raw(xd).cpu().numpy()
     assert E.status() == 0
     assert rel(y1, y0) <= 1e-5, rel(y1, y0)
+    # an output buffer 4 bytes off 16-byte alignment takes the mma.sync path
+    buf = torch.empty(y1.size + 1, dtype=torch.float32, device="cuda")
+    _lib.check(E.lib.pc_mlp_forward(E.h, xd.data_ptr(), x.shape[1], buf[1:].data_ptr(), E._stream()),
+               "pc_mlp_forward")
+    assert rel(buf[1:].cpu().numpy().reshape(y1.shape), y0) <= 1e-6
     for m in range(E.members):
         want, _ = mlp64.forward(p[m], x[m], DIMS)
         assert rel(y1[m], want) <= 1e-2
