@@ -76,10 +76,14 @@ struct PsiPoint {
 };
 
 // RPT = 2 rows per consumer thread: rows warp and warp + TY/2 of the tile.
-template <typename T, int TY, int TZ, int S, bool CPML, bool HCOEF, bool CA>
+// AX: the CPML axes this variant handles (bit 0 x, bit 1 y, bit 2 z; 0 = no CPML
+// code); the host gives a variant only items whose planes and tile (with halo)
+// stay clear of the slabs of the other axes.
+template <typename T, int TY, int TZ, int S, int AX, bool HCOEF, bool CA>
 __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
     fused3(FieldArgs<T> a, CpmlArgs<T> pm, const int4* __restrict__ items, const __grid_constant__ FusedMaps maps) {
     using G = FusedGeom<T, TY, TZ>;
+    constexpr bool CPML = AX != 0, CX = (AX & 1) != 0, CY = (AX & 2) != 0, CZ = (AX & 4) != 0;
     constexpr int EW = G::EW, HW = G::HW, NW = G::NW;
     constexpr int NWC = TY / 2;  // consumer warps
     static_assert(TZ == 32, "one warp spans the tile in k");
@@ -182,15 +186,15 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
     auto fetch = [&](const PsiPoint<T>& q, bool isH, T* v) {
 #pragma unroll
         for (int w = 0; w < 6; ++w) v[w] = T(0);
-        if (q.sx >= 0) {
+        if (CX && q.sx >= 0) {
             v[0] = ld(q.ox + (isH ? xA_H : xA_E));
             v[1] = ld(q.ox + (isH ? xB_H : xB_E));
         }
-        if (q.sy >= 0) {
+        if (CY && q.sy >= 0) {
             v[2] = ld(q.oy + (isH ? yA_H : yA_E));
             v[3] = ld(q.oy + (isH ? yB_H : yB_E));
         }
-        if (q.sz >= 0) {
+        if (CZ && q.sz >= 0) {
             v[4] = ld(q.oz + (isH ? zA_H : zA_E));
             v[5] = ld(q.oz + (isH ? zB_H : zB_E));
         }
@@ -221,8 +225,8 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
         pho[r] = jj * HW + kk;
         pno[r] = jj * NW + kk;
         pin[r] = exists && pj[r] < ny && pk[r] < nz;
-        psy[r] = pin[r] ? sl_of(pj[r], ny) : -1;
-        psz[r] = pin[r] ? sl_of(pk[r], nz) : -1;
+        psy[r] = (CY && pin[r]) ? sl_of(pj[r], ny) : -1;
+        psz[r] = (CZ && pin[r]) ? sl_of(pk[r], nz) : -1;
         coef3(1, psy[r], pyb[r], pya[r], pyk[r]);
         coef3(2, psz[r], pzb[r], pza[r], pzk[r]);
         poxc[r] = (int)pm.axis_base[0] + pj[r] * P32 + pk[r];
@@ -240,7 +244,7 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
         for (int r = 0; r < 2; ++r) {
             if (!pin[r]) continue;
             const int64_t lo_x = poxc[r], hi_x = (int64_t)poxc[r] + (int64_t)(t2 - 1) * ny * P32 + sxm;
-            bool ok = lo_x >= 0 && hi_x < tot;
+            bool ok = !CX || (lo_x >= 0 && hi_x < tot);
             if (psy[r] >= 0) ok = ok && poyc[r] >= 0 && (int64_t)poyc[r] + phi * t2 * P32 + sym < tot;
             if (psz[r] >= 0) ok = ok && pozc[r] >= 0 && (int64_t)pozc[r] + phi * ny * t2 + szm < tot;
             psi_ok = psi_ok && ok;
@@ -249,13 +253,13 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
     }
     const int k = k0 + lane;  // consumers' own k
     auto pt_at = [&](int pl, int r) {
-        return make_pt(pl, pin[r] ? sl_of(pl, nx) : -1, psy[r], psz[r], poxc[r], poyc[r], pozc[r]);
+        return make_pt(pl, (CX && pin[r]) ? sl_of(pl, nx) : -1, psy[r], psz[r], poxc[r], poyc[r], pozc[r]);
     };
     auto og = [&](int pl, int r) { return (int64_t)pl * PR + (int64_t)pj[r] * P + pk[r]; };
     // CTA-uniform: does the tile touch a y or z slab (then every plane needs CPML)?
     // (the +1 halo row/column of H counts: E at the tile edge reads it)
-    const bool yz_slab = CPML && (j0 < t || j0 + TY >= ny - t || k0 < t || k0 + TZ >= nz - t);
-    auto x_slab = [&](int pl) { return CPML && pl >= 0 && pl < nx && (pl < t || pl >= nx - t); };
+    const bool yz_slab = (CY && (j0 < t || j0 + TY >= ny - t)) || (CZ && (k0 < t || k0 + TZ >= nz - t));
+    auto x_slab = [&](int pl) { return CX && pl >= 0 && pl < nx && (pl < t || pl >= nx - t); };
 
     // ---- H^{n+1/2} at one point --------------------------------------------
     auto h_compute = [&](const T* E0, const T* E1, const T* E2, const T* Ep1, const T* Ep2, const T* H0,
@@ -277,19 +281,19 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
         T d4 = (ey - E1[ei - 1]) * idz;
         T d5 = (ex - E0[ei - 1]) * idz;
         if (CPML && slab) {
-            if (q.sx >= 0) {
+            if (CX && q.sx >= 0) {
                 d0 = pstep(xb, xa, xk, d0, v[0]);
                 d1 = pstep(xb, xa, xk, d1, v[1]);
                 if (own && uy) st(q.ox + xA_H, v[0]);
                 if (own && uz) st(q.ox + xB_H, v[1]);
             }
-            if (q.sy >= 0) {
+            if (CY && q.sy >= 0) {
                 d2 = pstep(b1, a1, k1, d2, v[2]);
                 d3 = pstep(b1, a1, k1, d3, v[3]);
                 if (own && ux) st(q.oy + yA_H, v[2]);
                 if (own && uz) st(q.oy + yB_H, v[3]);
             }
-            if (q.sz >= 0) {
+            if (CZ && q.sz >= 0) {
                 d4 = pstep(b2, a2, k2, d4, v[4]);
                 d5 = pstep(b2, a2, k2, d5, v[5]);
                 if (own && ux) st(q.oz + zA_H, v[4]);
@@ -346,7 +350,7 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
         const T* Cq = reinterpret_cast<const T*>(stp + 3 * (G::E_BOX + G::H_BOX));
         // x-slab coefficients of planes p and q (uniform)
         T xbH = T(1), xaH = T(0), xkH = T(1), xbE = T(1), xaE = T(0), xkE = T(1);
-        if (CPML) {
+        if (CX) {
             coef3(0, sl_of(p, nx), xbH, xaH, xkH);
             coef3(0, sl_of(q, nx), xbE, xaE, xkE);
         }
@@ -400,19 +404,19 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
                     if (CPML && slabE) {
                         const PsiPoint<T> pt = pt_at(q, r);
                         T* v = pfE[r];
-                        if (pt.sx >= 0) {
+                        if (CX && pt.sx >= 0) {
                             d0 = pstep(xbE, xaE, xkE, d0, v[0]);
                             d1 = pstep(xbE, xaE, xkE, d1, v[1]);
                             if (uy) st(pt.ox + xA_E, v[0]);
                             if (uz) st(pt.ox + xB_E, v[1]);
                         }
-                        if (pt.sy >= 0) {
+                        if (CY && pt.sy >= 0) {
                             d2 = pstep(pyb[r], pya[r], pyk[r], d2, v[2]);
                             d3 = pstep(pyb[r], pya[r], pyk[r], d3, v[3]);
                             if (ux) st(pt.oy + yA_E, v[2]);
                             if (uz) st(pt.oy + yB_E, v[3]);
                         }
-                        if (pt.sz >= 0) {
+                        if (CZ && pt.sz >= 0) {
                             d4 = pstep(pzb[r], pza[r], pzk[r], d4, v[4]);
                             d5 = pstep(pzb[r], pza[r], pzk[r], d5, v[5]);
                             if (ux) st(pt.oz + zA_E, v[4]);
@@ -495,15 +499,21 @@ int make_map(CUtensorMap* m, const void* base, const pc_grid_desc& g, int bw, in
     return r == CUDA_SUCCESS ? PC_OK : PC_ERR_CUDA;
 }
 
+// Work-item classes of one step, each launched as its own kernel variant.
+enum { CL_PLAIN, CL_GEN, CL_Z, CL_Y, CL_X, CL_N };
+constexpr int kClassAxes[CL_N] = {0, 7, 4, 2, 1};
+
 struct FusedState {
     const void* key_f[2][6];
     const void* key_cb[3];
     FusedMaps maps[2];  // per input set
     bool ready = false;
-    int4* d_items = nullptr;  // work items of the current chunking: plain ones, then cpml ones
-    int n_items = 0, n_plain = 0, items_cx = -1, items_t = -1;
-    cudaStream_t side = nullptr;  // the cpml class runs here, concurrently with the plain class
-    cudaEvent_t fork = nullptr, join = nullptr;
+    int4* d_items = nullptr;  // work items of the current chunking, class after class
+    int n_cls[CL_N] = {}, off_cls[CL_N] = {};
+    int items_cx = -1, items_t = -1, items_split = -1;
+    // the CPML classes run here, concurrently with the plain class and each other
+    cudaStream_t side[CL_N - 1] = {};
+    cudaEvent_t fork = nullptr, join[CL_N - 1] = {};
 };
 
 // One cached set of maps per context (keyed by the buffer pointers).
@@ -513,15 +523,15 @@ FusedState* state_of(pc_ctx* c) {
 }
 
 // Work items (k0, j0, ib, ie) for a chunk length cx, most expensive first
-// (longest-processing-time-first ordering against the tail).  With a CPML the
-// items fall in two classes that run as separate launches:
-//   plain: the tile and its +1 halo row/column lie outside every y/z slab and the
-//          planes [ib, ie] (ie = halo plane) outside the x slabs -> the kernel
-//          variant without CPML code;
-//   cpml:  everything else (x-chunks [0, t) and [nx-t-1, nx) of every tile, and
-//          every chunk of tiles that touch a y or z slab).
-static void fused_items(const pc_grid_desc& g, int TY, int TZ, int cx, int t, std::vector<int4>& plain,
-                        std::vector<int4>& cpml) {
+// (longest-processing-time-first ordering against the tail).  With a CPML an item
+// touches the slabs of a set of axes: x when its planes [ib, ie] (ie = halo plane)
+// reach an x slab, y / z when its tile with the +1 halo row / column reaches a y /
+// z slab.  Items that touch none run the variant without CPML code (CL_PLAIN);
+// with `split`, items that touch exactly one axis run that axis's variant (CL_X,
+// CL_Y, CL_Z: the x-chunks [0, t) and [nx-t-1, nx) of inner tiles, the edge tiles
+// of the inner planes), and the rest (corners, edges) the general one (CL_GEN).
+static void fused_items(const pc_grid_desc& g, int TY, int TZ, int cx, int t, bool split,
+                        std::vector<int4> (&cls)[CL_N]) {
     std::vector<std::pair<int, int>> chunks;
     if (t > 0 && g.nx > 2 * t + 2) {
         chunks.push_back({0, t});
@@ -530,36 +540,42 @@ static void fused_items(const pc_grid_desc& g, int TY, int TZ, int cx, int t, st
     } else {
         for (int ib = 0; ib < g.nx; ib += cx) chunks.push_back({ib, std::min(g.nx, ib + cx)});
     }
-    std::vector<std::pair<double, int4>> vp, vc;
+    std::vector<std::pair<double, int4>> v[CL_N];
     for (auto& ch : chunks) {
         const int ib = ch.first, ie = ch.second;
         const bool xs = t > 0 && (ib < t || ie >= g.nx - t);
         for (int j0 = 0; j0 < g.ny; j0 += TY)
             for (int k0 = 0; k0 < g.nz; k0 += TZ) {
-                const bool yz = t > 0 && (j0 < t || j0 + TY >= g.ny - t || k0 < t || k0 + TZ >= g.nz - t);
+                const bool ys = t > 0 && (j0 < t || j0 + TY >= g.ny - t);
+                const bool zs = t > 0 && (k0 < t || k0 + TZ >= g.nz - t);
+                const int mask = (xs ? 1 : 0) | (ys ? 2 : 0) | (zs ? 4 : 0);
+                int c = CL_GEN;
+                if (mask == 0)
+                    c = CL_PLAIN;
+                else if (split && mask == 4)
+                    c = CL_Z;
+                else if (split && mask == 2)
+                    c = CL_Y;
+                else if (split && mask == 1)
+                    c = CL_X;
                 const double planes = ie - ib + 2;
-                const int4 it = make_int4(k0, j0, ib, ie);
-                if (t > 0 && (yz || xs))
-                    vc.push_back({yz ? 3.0 * planes : 2.5 * planes, it});
-                else
-                    vp.push_back({planes, it});
+                v[c].push_back({mask == 0 ? planes : ((ys || zs) ? 3.0 : 2.5) * planes, make_int4(k0, j0, ib, ie)});
             }
     }
     auto by_cost = [](const std::pair<double, int4>& x, const std::pair<double, int4>& y) {
         return x.first > y.first;
     };
-    std::stable_sort(vp.begin(), vp.end(), by_cost);
-    std::stable_sort(vc.begin(), vc.end(), by_cost);
-    plain.clear();
-    cpml.clear();
-    for (auto& e : vp) plain.push_back(e.second);
-    for (auto& e : vc) cpml.push_back(e.second);
+    for (int c = 0; c < CL_N; ++c) {
+        std::stable_sort(v[c].begin(), v[c].end(), by_cost);
+        cls[c].clear();
+        for (auto& e : v[c]) cls[c].push_back(e.second);
+    }
 }
 
-template <typename T, int TY, int TZ, int S, bool CPML, bool HCOEF, bool CA>
+template <typename T, int TY, int TZ, int S, int AX, bool HCOEF, bool CA>
 int launch_variant(cudaStream_t s, const FieldArgs<T>& a, const CpmlArgs<T>& p, const FusedMaps& maps, int smem,
                    const int4* items, int n_items) {
-    auto kern = fused3<T, TY, TZ, S, CPML, HCOEF, CA>;
+    auto kern = fused3<T, TY, TZ, S, AX, HCOEF, CA>;
     static bool attr = false;
     if (!attr) {  // the largest size any launch asks for (CPML table for PC_MAX_CPML)
         const int smem_max = fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * PC_MAX_CPML * (int)sizeof(T);
@@ -576,7 +592,7 @@ int launch_variant(cudaStream_t s, const FieldArgs<T>& a, const CpmlArgs<T>& p, 
 // chunk length along x: enough work items for ~8 per resident CTA slot
 template <typename T, int TY, int TZ, int S>
 int choose_chunk(const pc_grid_desc& g, int smem) {
-    auto kern = fused3<T, TY, TZ, S, true, false, false>;
+    auto kern = fused3<T, TY, TZ, S, 7, false, false>;
     constexpr int threads = TZ * (TY / 2 + 1);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
@@ -635,61 +651,86 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
     const FusedMaps& m = st->maps[in];
     if (c->fused_cx <= 0) c->fused_cx = choose_chunk<T, TY, TZ, S>(g, smem);
     const int cx = c->fused_cx;
-    if (st->items_cx != cx || st->items_t != p.t || !st->d_items) {
-        std::vector<int4> plain, cpml;
-        fused_items(g, TY, TZ, cx, p.t, plain, cpml);
-        plain.insert(plain.end(), cpml.begin(), cpml.end());
+    const int kp = (hc ? 2 : 0) | (ca ? 1 : 0);
+    // single-axis classes: float without per-cell H or Ca coefficients (each class
+    // is one more kernel instantiation); otherwise every CPML item is general
+    const bool split = sizeof(T) == 4 && kp == 0;
+    if (st->items_cx != cx || st->items_t != p.t || st->items_split != (int)split || !st->d_items) {
+        std::vector<int4> cls[CL_N], all;
+        fused_items(g, TY, TZ, cx, p.t, split, cls);
+        for (int q = 0; q < CL_N; ++q) {
+            st->off_cls[q] = (int)all.size();
+            st->n_cls[q] = (int)cls[q].size();
+            all.insert(all.end(), cls[q].begin(), cls[q].end());
+        }
         cudaFree(st->d_items);
         st->d_items = nullptr;
-        PC_CUDA_CHECK(cudaMalloc(&st->d_items, plain.size() * sizeof(int4)));
-        PC_CUDA_CHECK(cudaMemcpy(st->d_items, plain.data(), plain.size() * sizeof(int4), cudaMemcpyHostToDevice));
-        st->n_items = (int)plain.size();
-        st->n_plain = (int)(plain.size() - cpml.size());
+        PC_CUDA_CHECK(cudaMalloc(&st->d_items, all.size() * sizeof(int4)));
+        PC_CUDA_CHECK(cudaMemcpy(st->d_items, all.data(), all.size() * sizeof(int4), cudaMemcpyHostToDevice));
         st->items_cx = cx;
         st->items_t = p.t;
+        st->items_split = (int)split;
     }
-    const int4* it_plain = st->d_items;
-    const int4* it_cpml = st->d_items + st->n_plain;
-    const int n_plain = st->n_plain, n_cpml = st->n_items - st->n_plain;
-    cudaStream_t sc = s;  // stream of the cpml class
-    if (cp && n_plain > 0 && n_cpml > 0) {
-        if (!st->side) {
+    const int n_plain = st->n_cls[CL_PLAIN];
+    int n_side = 0;  // CPML classes with items
+    for (int q = CL_GEN; q < CL_N; ++q) n_side += st->n_cls[q] > 0;
+    const bool fork = cp && n_side > 0 && (n_plain > 0 || n_side > 1);
+    if (fork) {
+        if (!st->fork) {
             // highest priority: the slab items are the long ones, so their CTAs are
             // dispatched first and the plain items fill in behind them
             int lo = 0, hi = 0;
             PC_CUDA_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-            PC_CUDA_CHECK(cudaStreamCreateWithPriority(&st->side, cudaStreamNonBlocking, hi));
+            for (int q = 0; q < CL_N - 1; ++q) {
+                PC_CUDA_CHECK(cudaStreamCreateWithPriority(&st->side[q], cudaStreamNonBlocking, hi));
+                PC_CUDA_CHECK(cudaEventCreateWithFlags(&st->join[q], cudaEventDisableTiming));
+            }
             PC_CUDA_CHECK(cudaEventCreateWithFlags(&st->fork, cudaEventDisableTiming));
-            PC_CUDA_CHECK(cudaEventCreateWithFlags(&st->join, cudaEventDisableTiming));
         }
         PC_CUDA_CHECK(cudaEventRecord(st->fork, s));
-        PC_CUDA_CHECK(cudaStreamWaitEvent(st->side, st->fork, 0));
-        sc = st->side;
     }
-    int rc;
-    const int kp = (hc ? 2 : 0) | (ca ? 1 : 0);
-    if (cp) {  // the slab class first (see the side stream's priority)
-        switch (kp) {
-            case 0: rc = launch_variant<T, TY, TZ, S, true, false, false>(sc, a, p, m, smem, it_cpml, n_cpml); break;
-            case 1: rc = launch_variant<T, TY, TZ, S, true, false, true>(sc, a, p, m, smem, it_cpml, n_cpml); break;
-            case 2: rc = launch_variant<T, TY, TZ, S, true, true, false>(sc, a, p, m, smem, it_cpml, n_cpml); break;
-            default: rc = launch_variant<T, TY, TZ, S, true, true, true>(sc, a, p, m, smem, it_cpml, n_cpml); break;
+    int rc = PC_OK;
+    if (cp) {  // the slab classes first (see the side streams' priority)
+        for (int q = CL_GEN; q < CL_N && !rc; ++q) {
+            const int n = st->n_cls[q];
+            if (n <= 0) continue;
+            cudaStream_t sq = s;
+            if (fork) {
+                sq = st->side[q - 1];
+                PC_CUDA_CHECK(cudaStreamWaitEvent(sq, st->fork, 0));
+            }
+            const int4* it = st->d_items + st->off_cls[q];
+            if (q == CL_GEN) {
+                switch (kp) {
+                    case 0: rc = launch_variant<T, TY, TZ, S, 7, false, false>(sq, a, p, m, smem, it, n); break;
+                    case 1: rc = launch_variant<T, TY, TZ, S, 7, false, true>(sq, a, p, m, smem, it, n); break;
+                    case 2: rc = launch_variant<T, TY, TZ, S, 7, true, false>(sq, a, p, m, smem, it, n); break;
+                    default: rc = launch_variant<T, TY, TZ, S, 7, true, true>(sq, a, p, m, smem, it, n); break;
+                }
+            } else if constexpr (sizeof(T) == 4) {  // split classes exist only for float, kp == 0
+                if (q == CL_Z) rc = launch_variant<T, TY, TZ, S, 4, false, false>(sq, a, p, m, smem, it, n);
+                if (q == CL_Y) rc = launch_variant<T, TY, TZ, S, 2, false, false>(sq, a, p, m, smem, it, n);
+                if (q == CL_X) rc = launch_variant<T, TY, TZ, S, 1, false, false>(sq, a, p, m, smem, it, n);
+            } else {
+                rc = PC_ERR_INVALID;
+            }
+            if (fork) PC_CUDA_CHECK(cudaEventRecord(st->join[q - 1], sq));
+            ++c->launches;
         }
         if (rc) return rc;
-        if (n_cpml > 0) ++c->launches;
     }
     // the plain class (no CPML code) on the caller's stream
+    const int4* it_plain = st->d_items + st->off_cls[CL_PLAIN];
     switch (kp) {
-        case 0: rc = launch_variant<T, TY, TZ, S, false, false, false>(s, a, p, m, smem, it_plain, n_plain); break;
-        case 1: rc = launch_variant<T, TY, TZ, S, false, false, true>(s, a, p, m, smem, it_plain, n_plain); break;
-        case 2: rc = launch_variant<T, TY, TZ, S, false, true, false>(s, a, p, m, smem, it_plain, n_plain); break;
-        default: rc = launch_variant<T, TY, TZ, S, false, true, true>(s, a, p, m, smem, it_plain, n_plain); break;
+        case 0: rc = launch_variant<T, TY, TZ, S, 0, false, false>(s, a, p, m, smem, it_plain, n_plain); break;
+        case 1: rc = launch_variant<T, TY, TZ, S, 0, false, true>(s, a, p, m, smem, it_plain, n_plain); break;
+        case 2: rc = launch_variant<T, TY, TZ, S, 0, true, false>(s, a, p, m, smem, it_plain, n_plain); break;
+        default: rc = launch_variant<T, TY, TZ, S, 0, true, true>(s, a, p, m, smem, it_plain, n_plain); break;
     }
     if (rc) return rc;
-    if (sc != s) {
-        PC_CUDA_CHECK(cudaEventRecord(st->join, sc));
-        PC_CUDA_CHECK(cudaStreamWaitEvent(s, st->join, 0));
-    }
+    if (fork)
+        for (int q = CL_GEN; q < CL_N; ++q)
+            if (st->n_cls[q] > 0) PC_CUDA_CHECK(cudaStreamWaitEvent(s, st->join[q - 1], 0));
     if (n_plain > 0) ++c->launches;
     c->cur = out;
     return PC_OK;
@@ -730,7 +771,7 @@ int noalloc_run(const pc_grid_desc& g, void* const set0[6], void* const set1[6],
                 int nsteps, cudaStream_t s, int4* scratch) {
     constexpr int TY = 16, TZ = 32, S = (sizeof(T) == 4) ? 4 : 3;
     using G = FusedGeom<T, TY, TZ>;
-    auto kern = fused3<T, TY, TZ, S, false, false, false>;
+    auto kern = fused3<T, TY, TZ, S, 0, false, false>;
     const int smem = fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * PC_MAX_CPML * (int)sizeof(T);
     PC_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     const int ntk = (g.nz + TZ - 1) / TZ, ntj = (g.ny + TY - 1) / TY;
@@ -846,9 +887,11 @@ void destroy_fused_state(pc_ctx* c) {
     if (c->fused_state) {
         FusedState* st = static_cast<FusedState*>(c->fused_state);
         cudaFree(st->d_items);
-        if (st->side) cudaStreamDestroy(st->side);
+        for (int q = 0; q < CL_N - 1; ++q) {
+            if (st->side[q]) cudaStreamDestroy(st->side[q]);
+            if (st->join[q]) cudaEventDestroy(st->join[q]);
+        }
         if (st->fork) cudaEventDestroy(st->fork);
-        if (st->join) cudaEventDestroy(st->join);
     }
     delete static_cast<FusedState*>(c->fused_state);
     c->fused_state = nullptr;

@@ -214,8 +214,11 @@ def test_fused_chunking_with_cpml_slabs(torch, chunk):
 
 @pytest.mark.parametrize("chunk", [0, 9])
 def test_fused_plain_and_cpml_item_classes(torch, chunk):
-    """Both item classes in one step (tiles clear of every slab run the variant
-    without CPML code, concurrently with the slab tiles), with tiles whose +1 H
+    """Every item class in one step: tiles clear of every slab (variant without
+    CPML code), in float32 tiles that touch only the x slabs (inner tiles of the
+    end chunks), only a y slab (j0 = 0, 48, 64 at k0 = 32), only a z slab (j0 = 16,
+    32 at k0 = 0, 64, 96) with their single-axis variants, the rest (and every
+    CPML item in float64) with the general one, concurrently; tiles whose +1 H
     halo row/column lands exactly on the first slab row/column (ny - t = 48 + 16,
     nz - t = 64 + 32)."""
     from prismo_gb300 import _lib
