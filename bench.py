@@ -323,7 +323,7 @@ def main():
                                    "32 seeded boxes eps U[1,12.11] on 2.085, Ez dipole 193THz/10fs",
                        "time_steps_per_step": tsteps, "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "inputs larger than L2 (fields 2x403 MB)", "status": status,
-                       "fused_chunk": tuned_chunk},
+                       "fused_chunk": None if tuned_chunk is None else list(tuned_chunk)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                          "bytes_per_cell_update": bpc, "kernel": "fused3 (H+E+CPML)",

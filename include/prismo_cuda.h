@@ -173,13 +173,23 @@ int pc_status(pc_ctx* ctx, uint32_t* flags, void* stream);
 int64_t pc_launch_count(const pc_ctx* ctx);
 
 /* Tuning knobs.  PC_TUNE_FUSED_CHUNK: planes along x streamed by one CTA of the
- * fused 3D schedule (0 = automatic choice).  PC_TUNE_GRAPH_STEPS: pc_step replays
+ * fused 3D schedule (0 = automatic choice).  PC_TUNE_FUSED_CHUNK_EDGE: the same
+ * for tiles that touch a y or z CPML slab (0 = PC_TUNE_FUSED_CHUNK).
+ * PC_TUNE_FUSED_SPLIT: which CPML work items get a kernel variant of their own
+ * slab axes (float32 without per-cell H or Ca coefficients): 0 none (one
+ * general variant), 1 items on one axis's slabs, 2 also items on two axes' slabs
+ * (default).  PC_TUNE_FUSED_UNIFIED: those variants run as one launch that picks
+ * the variant per work item (1, default) or as one launch per variant on
+ * concurrent streams (0).  PC_TUNE_GRAPH_STEPS: pc_step replays
  * its time loop from a CUDA graph of this many steps (a multiple of 16; 0 = one
  * launch sequence per step), captured on first use after an eager step and
  * re-captured after any call that changes what a step launches.  Steps with a
  * TFSF source or with pc_profile enabled always run eagerly.  Default 64. */
 #define PC_TUNE_FUSED_CHUNK 1
 #define PC_TUNE_GRAPH_STEPS 2
+#define PC_TUNE_FUSED_CHUNK_EDGE 3
+#define PC_TUNE_FUSED_SPLIT 4
+#define PC_TUNE_FUSED_UNIFIED 5
 int pc_set_tuning(pc_ctx* ctx, int32_t key, int64_t value);
 int64_t pc_get_tuning(const pc_ctx* ctx, int32_t key);
 

@@ -32,6 +32,9 @@ PC_SCHED_SPLIT = 1
 PC_SCHED_FUSED = 2
 
 PC_TUNE_FUSED_CHUNK = 1
+PC_TUNE_FUSED_CHUNK_EDGE = 3
+PC_TUNE_FUSED_SPLIT = 4
+PC_TUNE_FUSED_UNIFIED = 5
 PC_TUNE_GRAPH_STEPS = 2
 
 

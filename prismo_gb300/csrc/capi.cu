@@ -123,6 +123,8 @@ int pc_create(const pc_grid_desc* desc, pc_ctx** out) {
     c->gen = 1;
     c->warm_gen = 0;
     c->graph_steps = 64;
+    c->fused_split = 2;
+    c->fused_unified = 1;
     c->graph_gen[0] = c->graph_gen[1] = 0;
     if (cudaMalloc(&c->d_status, 2 * sizeof(uint32_t)) != cudaSuccess) {
         delete c;
@@ -563,6 +565,18 @@ int pc_set_tuning(pc_ctx* c, int32_t key, int64_t value) {
             if (value < 0 || value > c->g.nx) return PC_ERR_INVALID;
             c->fused_cx = (int)value;
             return PC_OK;
+        case PC_TUNE_FUSED_CHUNK_EDGE:
+            if (value < 0 || value > c->g.nx) return PC_ERR_INVALID;
+            c->fused_cx_edge = (int)value;
+            return PC_OK;
+        case PC_TUNE_FUSED_SPLIT:
+            if (value < 0 || value > 2) return PC_ERR_INVALID;
+            c->fused_split = (int)value;
+            return PC_OK;
+        case PC_TUNE_FUSED_UNIFIED:
+            if (value < 0 || value > 1) return PC_ERR_INVALID;
+            c->fused_unified = (int)value;
+            return PC_OK;
         case PC_TUNE_GRAPH_STEPS:
             if (value < 0 || value % 16 != 0 || value > (1 << 20)) return PC_ERR_INVALID;
             c->graph_steps = (int)value;
@@ -575,6 +589,9 @@ int pc_set_tuning(pc_ctx* c, int32_t key, int64_t value) {
 int64_t pc_get_tuning(const pc_ctx* c, int32_t key) {
     if (!c) return PC_ERR_INVALID;
     if (key == PC_TUNE_FUSED_CHUNK) return c->fused_cx;
+    if (key == PC_TUNE_FUSED_CHUNK_EDGE) return c->fused_cx_edge;
+    if (key == PC_TUNE_FUSED_SPLIT) return c->fused_split;
+    if (key == PC_TUNE_FUSED_UNIFIED) return c->fused_unified;
     if (key == PC_TUNE_GRAPH_STEPS) return c->graph_steps;
     return PC_ERR_INVALID;
 }

@@ -143,6 +143,9 @@ struct pc_ctx {
     // fused schedule: cached tensor maps and the chosen x-chunk length
     void* fused_state;
     int fused_cx;
+    int fused_cx_edge;  // x-chunk of tiles that touch a y or z slab (0: fused_cx)
+    int fused_split;    // CPML item classes: 0 general only, 1 + single-axis, 2 + two-axis (default)
+    int fused_unified;  // every class in one launch (1, default) or one launch per class (0)
     // optional CUDA-event timing of the main stencil launch of every step
     bool prof_on;
     std::vector<cudaEvent_t> prof_ev;  // start/stop pairs, recycled

@@ -75,13 +75,17 @@ struct PsiPoint {
     int ox, oy, oz;
 };
 
-// RPT = 2 rows per consumer thread: rows warp and warp + TY/2 of the tile.
-// AX: the CPML axes this variant handles (bit 0 x, bit 1 y, bit 2 z; 0 = no CPML
-// code); the host gives a variant only items whose planes and tile (with halo)
-// stay clear of the slabs of the other axes.
+// Work-item classes of one step: items whose planes and tile (with its +1 halo)
+// touch the CPML slabs of no axis, of every axis, or of exactly the named ones.
+enum { CL_PLAIN, CL_GEN, CL_YZ, CL_XZ, CL_XY, CL_Z, CL_Y, CL_X, CL_N };
+
+// One work item of the fused step.  RPT = 2 rows per consumer thread: rows warp and
+// warp + TY/2 of the tile.  AX: the CPML axes this variant handles (bit 0 x, bit 1
+// y, bit 2 z; 0 = no CPML code); the host gives a variant only items whose planes
+// and tile (with halo) stay clear of the slabs of the other axes.
 template <typename T, int TY, int TZ, int S, int AX, bool HCOEF, bool CA>
-__global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
-    fused3(FieldArgs<T> a, CpmlArgs<T> pm, const int4* __restrict__ items, const __grid_constant__ FusedMaps maps) {
+__device__ __forceinline__ void fused3_item(const FieldArgs<T>& a, const CpmlArgs<T>& pm, const int4 item,
+                                            const FusedMaps& maps) {
     using G = FusedGeom<T, TY, TZ>;
     constexpr bool CPML = AX != 0, CX = (AX & 1) != 0, CY = (AX & 2) != 0, CZ = (AX & 4) != 0;
     constexpr int EW = G::EW, HW = G::HW, NW = G::NW;
@@ -99,8 +103,7 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
     const int lane = threadIdx.x, warp = threadIdx.y;
     const int tid = warp * 32 + lane;
     const bool helper = warp == NWC;
-    // work item: (k0, j0, first plane, one past the last plane), longest first
-    const int4 item = items[blockIdx.x];
+    // work item: (k0, j0, first plane, one past the last plane)
     const int k0 = item.x, j0 = item.y;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const int ib = item.z;
@@ -467,6 +470,34 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
     }
 }
 
+// one kernel variant: items[blockIdx.x], longest first
+template <typename T, int TY, int TZ, int S, int AX, bool HCOEF, bool CA>
+__global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
+    fused3(FieldArgs<T> a, CpmlArgs<T> pm, const int4* __restrict__ items, const __grid_constant__ FusedMaps maps) {
+    fused3_item<T, TY, TZ, S, AX, HCOEF, CA>(a, pm, items[blockIdx.x], maps);
+}
+
+// Every class in one launch (float32, no per-cell H or Ca coefficients): the class
+// of an item sits in the top byte of its w; the CTA runs that class's variant.
+template <typename T, int TY, int TZ, int S>
+__global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
+    fused3_multi(FieldArgs<T> a, CpmlArgs<T> pm, const int4* __restrict__ items,
+                 const __grid_constant__ FusedMaps maps) {
+    int4 it = items[blockIdx.x];
+    const int cls = it.w >> 24;
+    it.w &= 0xFFFFFF;
+    switch (cls) {
+        case CL_PLAIN: fused3_item<T, TY, TZ, S, 0, false, false>(a, pm, it, maps); break;
+        case CL_Z: fused3_item<T, TY, TZ, S, 4, false, false>(a, pm, it, maps); break;
+        case CL_Y: fused3_item<T, TY, TZ, S, 2, false, false>(a, pm, it, maps); break;
+        case CL_X: fused3_item<T, TY, TZ, S, 1, false, false>(a, pm, it, maps); break;
+        case CL_YZ: fused3_item<T, TY, TZ, S, 6, false, false>(a, pm, it, maps); break;
+        case CL_XZ: fused3_item<T, TY, TZ, S, 5, false, false>(a, pm, it, maps); break;
+        case CL_XY: fused3_item<T, TY, TZ, S, 3, false, false>(a, pm, it, maps); break;
+        default: fused3_item<T, TY, TZ, S, 7, false, false>(a, pm, it, maps); break;
+    }
+}
+
 using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                               const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -499,9 +530,6 @@ int make_map(CUtensorMap* m, const void* base, const pc_grid_desc& g, int bw, in
     return r == CUDA_SUCCESS ? PC_OK : PC_ERR_CUDA;
 }
 
-// Work-item classes of one step, each launched as its own kernel variant.
-enum { CL_PLAIN, CL_GEN, CL_Z, CL_Y, CL_X, CL_N };
-constexpr int kClassAxes[CL_N] = {0, 7, 4, 2, 1};
 
 struct FusedState {
     const void* key_f[2][6];
@@ -510,7 +538,7 @@ struct FusedState {
     bool ready = false;
     int4* d_items = nullptr;  // work items of the current chunking, class after class
     int n_cls[CL_N] = {}, off_cls[CL_N] = {};
-    int items_cx = -1, items_t = -1, items_split = -1;
+    int items_cx = -1, items_cxe = -1, items_t = -1, items_split = -1, items_unified = -1;
     // the CPML classes run here, concurrently with the plain class and each other
     cudaStream_t side[CL_N - 1] = {};
     cudaEvent_t fork = nullptr, join[CL_N - 1] = {};
@@ -527,49 +555,58 @@ FusedState* state_of(pc_ctx* c) {
 // touches the slabs of a set of axes: x when its planes [ib, ie] (ie = halo plane)
 // reach an x slab, y / z when its tile with the +1 halo row / column reaches a y /
 // z slab.  Items that touch none run the variant without CPML code (CL_PLAIN);
-// with `split`, items that touch exactly one axis run that axis's variant (CL_X,
-// CL_Y, CL_Z: the x-chunks [0, t) and [nx-t-1, nx) of inner tiles, the edge tiles
-// of the inner planes), and the rest (corners, edges) the general one (CL_GEN).
-static void fused_items(const pc_grid_desc& g, int TY, int TZ, int cx, int t, bool split,
-                        std::vector<int4> (&cls)[CL_N]) {
-    std::vector<std::pair<int, int>> chunks;
-    if (t > 0 && g.nx > 2 * t + 2) {
-        chunks.push_back({0, t});
-        for (int ib = t; ib < g.nx - t - 1; ib += cx) chunks.push_back({ib, std::min(g.nx - t - 1, ib + cx)});
-        chunks.push_back({g.nx - t - 1, g.nx});
-    } else {
-        for (int ib = 0; ib < g.nx; ib += cx) chunks.push_back({ib, std::min(g.nx, ib + cx)});
-    }
-    std::vector<std::pair<double, int4>> v[CL_N];
-    for (auto& ch : chunks) {
-        const int ib = ch.first, ie = ch.second;
-        const bool xs = t > 0 && (ib < t || ie >= g.nx - t);
-        for (int j0 = 0; j0 < g.ny; j0 += TY)
-            for (int k0 = 0; k0 < g.nz; k0 += TZ) {
-                const bool ys = t > 0 && (j0 < t || j0 + TY >= g.ny - t);
-                const bool zs = t > 0 && (k0 < t || k0 + TZ >= g.nz - t);
-                const int mask = (xs ? 1 : 0) | (ys ? 2 : 0) | (zs ? 4 : 0);
-                int c = CL_GEN;
-                if (mask == 0)
-                    c = CL_PLAIN;
-                else if (split && mask == 4)
-                    c = CL_Z;
-                else if (split && mask == 2)
-                    c = CL_Y;
-                else if (split && mask == 1)
-                    c = CL_X;
-                const double planes = ie - ib + 2;
-                v[c].push_back({mask == 0 ? planes : ((ys || zs) ? 3.0 : 2.5) * planes, make_int4(k0, j0, ib, ie)});
-            }
-    }
-    auto by_cost = [](const std::pair<double, int4>& x, const std::pair<double, int4>& y) {
-        return x.first > y.first;
+// with split >= 1, items that touch one axis run that axis's variant (CL_X, CL_Y,
+// CL_Z: the x-chunks [0, t) and [nx-t-1, nx) of inner tiles, the edge tiles of the
+// inner planes), with split 2 also items that touch two (CL_XY, CL_XZ: the end
+// chunks of edge tiles; CL_YZ: the corner tiles of the inner planes); the rest run
+// the general variant (CL_GEN).
+// relative cost of one tile-plane per class (warp instructions per tile-plane at
+// 256^3 over the plain class's): orders the items longest first
+constexpr double kClassCost[CL_N] = {1.0, 3.1, 2.6, 2.6, 2.6, 1.8, 1.7, 2.0};
+
+using CostItem = std::pair<double, int4>;
+
+// longest first; equal costs by chunk, then tile, so that neighbouring tiles of one
+// chunk run together and share their halo rows in L2
+static void sort_items(std::vector<CostItem>& v) {
+    std::sort(v.begin(), v.end(), [](const CostItem& x, const CostItem& y) {
+        if (x.first != y.first) return x.first > y.first;
+        if (x.second.z != y.second.z) return x.second.z < y.second.z;
+        if (x.second.y != y.second.y) return x.second.y < y.second.y;
+        return x.second.x < y.second.x;
+    });
+}
+
+static void fused_items(const pc_grid_desc& g, int TY, int TZ, int cx, int cx_edge, int t, int split,
+                        std::vector<CostItem> (&v)[CL_N]) {
+    auto chunking = [&](int c) {
+        std::vector<std::pair<int, int>> chunks;
+        if (t > 0 && g.nx > 2 * t + 2) {
+            chunks.push_back({0, t});
+            for (int ib = t; ib < g.nx - t - 1; ib += c) chunks.push_back({ib, std::min(g.nx - t - 1, ib + c)});
+            chunks.push_back({g.nx - t - 1, g.nx});
+        } else {
+            for (int ib = 0; ib < g.nx; ib += c) chunks.push_back({ib, std::min(g.nx, ib + c)});
+        }
+        return chunks;
     };
-    for (int c = 0; c < CL_N; ++c) {
-        std::stable_sort(v[c].begin(), v[c].end(), by_cost);
-        cls[c].clear();
-        for (auto& e : v[c]) cls[c].push_back(e.second);
-    }
+    const std::vector<std::pair<int, int>> inner = chunking(cx), edge = chunking(cx_edge);
+    for (int c = 0; c < CL_N; ++c) v[c].clear();
+    for (int j0 = 0; j0 < g.ny; j0 += TY)
+        for (int k0 = 0; k0 < g.nz; k0 += TZ) {
+            const bool ys = t > 0 && (j0 < t || j0 + TY >= g.ny - t);
+            const bool zs = t > 0 && (k0 < t || k0 + TZ >= g.nz - t);
+            for (auto& ch : (ys || zs) ? edge : inner) {
+                const int ib = ch.first, ie = ch.second;
+                const bool xs = t > 0 && (ib < t || ie >= g.nx - t);
+                const int mask = (xs ? 1 : 0) | (ys ? 2 : 0) | (zs ? 4 : 0);
+                static constexpr int by_mask[8] = {CL_PLAIN, CL_X, CL_Y, CL_XY, CL_Z, CL_XZ, CL_YZ, CL_GEN};
+                static constexpr int axes[8] = {0, 1, 1, 2, 1, 2, 2, 3};
+                const int c = (mask == 0 || axes[mask] <= split) ? by_mask[mask] : CL_GEN;
+                v[c].push_back({kClassCost[c] * (ie - ib + 2), make_int4(k0, j0, ib, ie)});
+            }
+        }
+    for (int c = 0; c < CL_N; ++c) sort_items(v[c]);
 }
 
 template <typename T, int TY, int TZ, int S, int AX, bool HCOEF, bool CA>
@@ -651,25 +688,43 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
     const FusedMaps& m = st->maps[in];
     if (c->fused_cx <= 0) c->fused_cx = choose_chunk<T, TY, TZ, S>(g, smem);
     const int cx = c->fused_cx;
+    const int cxe = c->fused_cx_edge > 0 ? c->fused_cx_edge : cx;
     const int kp = (hc ? 2 : 0) | (ca ? 1 : 0);
-    // single-axis classes: float without per-cell H or Ca coefficients (each class
+    // axis-specific classes: float without per-cell H or Ca coefficients (each class
     // is one more kernel instantiation); otherwise every CPML item is general
-    const bool split = sizeof(T) == 4 && kp == 0;
-    if (st->items_cx != cx || st->items_t != p.t || st->items_split != (int)split || !st->d_items) {
-        std::vector<int4> cls[CL_N], all;
-        fused_items(g, TY, TZ, cx, p.t, split, cls);
-        for (int q = 0; q < CL_N; ++q) {
-            st->off_cls[q] = (int)all.size();
-            st->n_cls[q] = (int)cls[q].size();
-            all.insert(all.end(), cls[q].begin(), cls[q].end());
+    const int split = (sizeof(T) == 4 && kp == 0) ? c->fused_split : 0;
+    // every class in one launch of fused3_multi (the class in the top byte of w)
+    const bool unified = split > 0 && c->fused_unified != 0 && cp;
+    if (st->items_cx != cx || st->items_cxe != cxe || st->items_t != p.t || st->items_split != (int)split ||
+        st->items_unified != (int)unified || !st->d_items) {
+        std::vector<CostItem> cls[CL_N];
+        std::vector<int4> all;
+        fused_items(g, TY, TZ, cx, cxe, p.t, split, cls);
+        if (unified) {
+            std::vector<CostItem> merged;
+            for (int q = 0; q < CL_N; ++q)
+                for (const CostItem& e : cls[q]) merged.push_back({e.first, make_int4(e.second.x, e.second.y,
+                                                                                      e.second.z, e.second.w | (q << 24))});
+            sort_items(merged);
+            for (const CostItem& e : merged) all.push_back(e.second);
+            for (int q = 0; q < CL_N; ++q) st->off_cls[q] = st->n_cls[q] = 0;
+            st->n_cls[CL_GEN] = (int)all.size();  // launched as one
+        } else {
+            for (int q = 0; q < CL_N; ++q) {
+                st->off_cls[q] = (int)all.size();
+                st->n_cls[q] = (int)cls[q].size();
+                for (const CostItem& e : cls[q]) all.push_back(e.second);
+            }
         }
         cudaFree(st->d_items);
         st->d_items = nullptr;
         PC_CUDA_CHECK(cudaMalloc(&st->d_items, all.size() * sizeof(int4)));
         PC_CUDA_CHECK(cudaMemcpy(st->d_items, all.data(), all.size() * sizeof(int4), cudaMemcpyHostToDevice));
         st->items_cx = cx;
+        st->items_cxe = cxe;
         st->items_t = p.t;
         st->items_split = (int)split;
+        st->items_unified = (int)unified;
     }
     const int n_plain = st->n_cls[CL_PLAIN];
     int n_side = 0;  // CPML classes with items
@@ -700,7 +755,20 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
                 PC_CUDA_CHECK(cudaStreamWaitEvent(sq, st->fork, 0));
             }
             const int4* it = st->d_items + st->off_cls[q];
-            if (q == CL_GEN) {
+            if (unified) {
+                if constexpr (sizeof(T) == 4) {
+                    static bool attr = false;
+                    if (!attr) {
+                        PC_CUDA_CHECK(cudaFuncSetAttribute(fused3_multi<T, TY, TZ, S>,
+                                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                           fused_smem_bytes<T, TY, TZ, S>() +
+                                                               9 * 2 * PC_MAX_CPML * (int)sizeof(T)));
+                        attr = true;
+                    }
+                    fused3_multi<T, TY, TZ, S><<<n, dim3(TZ, TY / 2 + 1), smem, sq>>>(a, p, it, m);
+                    PC_CUDA_CHECK(cudaGetLastError());
+                }
+            } else if (q == CL_GEN) {
                 switch (kp) {
                     case 0: rc = launch_variant<T, TY, TZ, S, 7, false, false>(sq, a, p, m, smem, it, n); break;
                     case 1: rc = launch_variant<T, TY, TZ, S, 7, false, true>(sq, a, p, m, smem, it, n); break;
@@ -708,9 +776,14 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
                     default: rc = launch_variant<T, TY, TZ, S, 7, true, true>(sq, a, p, m, smem, it, n); break;
                 }
             } else if constexpr (sizeof(T) == 4) {  // split classes exist only for float, kp == 0
-                if (q == CL_Z) rc = launch_variant<T, TY, TZ, S, 4, false, false>(sq, a, p, m, smem, it, n);
-                if (q == CL_Y) rc = launch_variant<T, TY, TZ, S, 2, false, false>(sq, a, p, m, smem, it, n);
-                if (q == CL_X) rc = launch_variant<T, TY, TZ, S, 1, false, false>(sq, a, p, m, smem, it, n);
+                switch (q) {
+                    case CL_YZ: rc = launch_variant<T, TY, TZ, S, 6, false, false>(sq, a, p, m, smem, it, n); break;
+                    case CL_XZ: rc = launch_variant<T, TY, TZ, S, 5, false, false>(sq, a, p, m, smem, it, n); break;
+                    case CL_XY: rc = launch_variant<T, TY, TZ, S, 3, false, false>(sq, a, p, m, smem, it, n); break;
+                    case CL_Z: rc = launch_variant<T, TY, TZ, S, 4, false, false>(sq, a, p, m, smem, it, n); break;
+                    case CL_Y: rc = launch_variant<T, TY, TZ, S, 2, false, false>(sq, a, p, m, smem, it, n); break;
+                    default: rc = launch_variant<T, TY, TZ, S, 1, false, false>(sq, a, p, m, smem, it, n); break;
+                }
             } else {
                 rc = PC_ERR_INVALID;
             }

@@ -360,11 +360,14 @@ class FDTDEngine:
         return float(ms.value), int(n.value)
 
     # -- autotuning ---------------------------------------------------------------
-    def autotune(self, candidates=(8, 16, 24, 32, 48, 64, 96), steps: int = 6, cache: bool = True):
-        """Pick the x-chunk length of the fused 3D schedule by timing a few steps of
-        each candidate with CUDA events; the fields and psi are restored afterwards.
-        Results are cached per (dims, CPML thickness, precision) in
-        ``$PRISMO_GB300_CACHE`` (default ~/.cache/prismo_gb300/tune.json)."""
+    def autotune(self, candidates=(8, 16, 24, 32, 48, 64, 96), steps: int = 20, cache: bool = True):
+        """Pick the x-chunk lengths of the fused 3D schedule by timing a few steps of
+        each candidate with CUDA events: first one length for every tile, then,
+        with that fixed for the inner tiles, the length for tiles that touch a y or
+        z CPML slab.  The fields and psi are restored afterwards.  Returns
+        (chunk, edge chunk).  Results are cached per (dims, CPML thickness,
+        precision) in ``$PRISMO_GB300_CACHE`` (default
+        ~/.cache/prismo_gb300/tune.json)."""
         import json
         import os
 
@@ -382,19 +385,18 @@ class FDTDEngine:
                     table = json.load(f)
             except (OSError, ValueError):
                 table = {}
-        if cache and key in table:
-            self.set_chunk(int(table[key]))
-            return int(table[key])
+        if cache and isinstance(table.get(key), list) and len(table[key]) == 2:
+            cx, ce = (int(v) for v in table[key])
+            self.set_chunk(cx, ce)
+            return cx, ce
         saved_sets = [t.clone() for t in self.sets]
         saved_psi = [t.clone() for t in self.psi]
         saved_cur = self.cur
-        best, best_ms = None, float("inf")
         nsrc = len(self.sources)
         amps = np.zeros((steps, nsrc)) if nsrc else None
-        for cx in candidates:
-            if cx >= self.dims[0]:
-                continue
-            self.set_chunk(cx)
+
+        def timed(cx, ce):
+            self.set_chunk(cx, ce)
             self.step(2, None if amps is None else amps[:2])
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
@@ -402,32 +404,62 @@ class FDTDEngine:
             self.step(steps, amps)
             e1.record(self.stream)
             e1.synchronize()
-            ms = e0.elapsed_time(e1)
+            return e0.elapsed_time(e1)
+
+        cands = [c for c in candidates if c < self.dims[0]]
+        best, best_ms = None, float("inf")
+        for cx in cands:
+            ms = timed(cx, 0)
             if ms < best_ms:
                 best, best_ms = cx, ms
+        best_e = 0
+        if best is not None and self.pml is not None:
+            for ce in cands:
+                if ce == best:
+                    continue
+                ms = timed(best, ce)
+                if ms < best_ms:
+                    best_e, best_ms = ce, ms
         for dst, src in zip(self.sets, saved_sets):
             dst.copy_(src)
         for dst, src in zip(self.psi, saved_psi):
             dst.copy_(src)
         _lib.check(self.lib.pc_set_current_set(self.ctx, saved_cur), "pc_set_current_set")
         self.check_status()
-        if best is not None:
-            self.set_chunk(best)
-            if cache:
-                table[key] = best
-                try:
-                    os.makedirs(os.path.dirname(path), exist_ok=True)
-                    with open(path, "w") as f:
-                        json.dump(table, f, indent=1)
-                except OSError:
-                    pass
-        return best
+        if best is None:
+            return None
+        self.set_chunk(best, best_e)
+        if cache:
+            table[key] = [best, best_e]
+            try:
+                os.makedirs(os.path.dirname(path), exist_ok=True)
+                with open(path, "w") as f:
+                    json.dump(table, f, indent=1)
+            except OSError:
+                pass
+        return best, best_e
 
-    def set_chunk(self, cx: int):
+    def set_chunk(self, cx: int, edge: int = 0):
+        """x-chunk length of the fused 3D schedule; `edge` for tiles that touch a y
+        or z CPML slab (0: the same as cx)."""
         _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_FUSED_CHUNK, int(cx)), "pc_set_tuning")
+        _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_FUSED_CHUNK_EDGE, int(edge)), "pc_set_tuning")
 
     def chunk(self) -> int:
         return int(self.lib.pc_get_tuning(self.ctx, _lib.PC_TUNE_FUSED_CHUNK))
+
+    def set_split(self, level: int, unified: Optional[bool] = None):
+        """CPML work items with a kernel variant of their own slab axes: 0 none, 1
+        items on one axis's slabs, 2 also items on two axes' slabs (default);
+        `unified`: all variants in one launch (default) instead of one launch per
+        variant on concurrent streams."""
+        _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_FUSED_SPLIT, int(level)), "pc_set_tuning")
+        if unified is not None:
+            _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_FUSED_UNIFIED, int(bool(unified))),
+                       "pc_set_tuning")
+
+    def chunk_edge(self) -> int:
+        return int(self.lib.pc_get_tuning(self.ctx, _lib.PC_TUNE_FUSED_CHUNK_EDGE))
 
     def set_graph_steps(self, n: int):
         """Steps per captured time-loop graph (a multiple of 16; 0 = eager steps)."""

@@ -212,13 +212,16 @@ def test_fused_chunking_with_cpml_slabs(torch, chunk):
     eng.close()
 
 
-@pytest.mark.parametrize("chunk", [0, 9])
-def test_fused_plain_and_cpml_item_classes(torch, chunk):
+@pytest.mark.parametrize("chunk,edge,split,unified", [(0, 0, 1, 0), (9, 0, 1, 0), (16, 5, 1, 0), (9, 0, 2, 0),
+                                                     (9, 0, 2, 1), (16, 5, 1, 1), (0, 0, 0, 0)])
+def test_fused_plain_and_cpml_item_classes(torch, chunk, edge, split, unified):
     """Every item class in one step: tiles clear of every slab (variant without
     CPML code), in float32 tiles that touch only the x slabs (inner tiles of the
     end chunks), only a y slab (j0 = 0, 48, 64 at k0 = 32), only a z slab (j0 = 16,
     32 at k0 = 0, 64, 96) with their single-axis variants, the rest (and every
-    CPML item in float64) with the general one, concurrently; tiles whose +1 H
+    CPML item in float64) with the general one, concurrently; split 2 adds the
+    two-axis variants, split 0 leaves only the general one; `unified` runs every
+    class from one launch; tiles whose +1 H
     halo row/column lands exactly on the first slab row/column (ny - t = 48 + 16,
     nz - t = 64 + 32)."""
     from prismo_gb300 import _lib
@@ -234,7 +237,8 @@ def test_fused_plain_and_cpml_item_classes(torch, chunk):
         eng = make_engine(g.dims, g.spacing, dt, False, precision=prec, sched="fused", material_arrays=mats,
                           pml=PMLParams(thickness=8))
         if chunk:
-            _lib.check(eng.lib.pc_set_tuning(eng.ctx, _lib.PC_TUNE_FUSED_CHUNK, chunk))
+            eng.set_chunk(chunk, edge)  # edge: chunk length of the tiles on a y/z slab
+        eng.set_split(split, bool(unified))
         load_fields(eng, init, torch)
         eng.step(30)
         out = read_fields(eng)
