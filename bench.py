@@ -57,13 +57,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profile():
-    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+def traffic_from_profile(dims):
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary
+    (None for a grid the summary does not cover)."""
     p = os.path.join(ROOT, "profiles", "fused3_256_cpml.json")
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
-        return d.get("dram_bytes_per_launch")
+        if tuple(d.get("dims", ())) == tuple(dims):
+            return d.get("dram_bytes_per_launch")
     return None
 
 
@@ -223,6 +225,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--chunk", default=None,
+                    help="x-chunk lengths 'CX[,EDGE]' of the fused schedule instead of autotuning (profiling runs)")
     ap.add_argument("--dims", type=int, default=None,
                     help="cube edge for a reduced profiling case (default: the 256^3 workload)")
     ap.add_argument("--workload", default="3d", choices=["3d", "2d", "dispersive", "sweep", "surrogate"],
@@ -262,7 +266,12 @@ def main():
         reset(eng)
         eng.step(tsteps, amps)
 
-    tuned_chunk = None if args.no_autotune else eng.autotune(cache=False)
+    if args.chunk:
+        cx, _, ce = args.chunk.partition(",")
+        eng.set_chunk(int(cx), int(ce or 0))
+        tuned_chunk = (int(cx), int(ce or 0))
+    else:
+        tuned_chunk = None if args.no_autotune else eng.autotune(cache=False)
     for _ in range(max(args.warmup, 3)):
         one()
     eng.synchronize()
@@ -301,7 +310,7 @@ def main():
     avg_launch_s = kern_ms / 1e3 / max(kern_n, 1)
     achieved = bpc * cells / avg_launch_s / 1e9  # GB/s
     peak, peak_kind = measured_peaks()
-    traffic = traffic_from_profile()
+    traffic = traffic_from_profile(DIMS)
 
     # end-to-end through the engine API with host buffers
     e2e = None
