@@ -119,8 +119,10 @@ __device__ __forceinline__ float h_plus(float h, float d, float da, float db) { 
 __device__ __forceinline__ float diff(float a, float b, float inv) { return __fmul_rn(__fsub_rn(a, b), inv); }
 
 // FAST: the kernel of the fast-path items (their own table and launch, with the
-// smaller shared-memory footprint and higher occupancy); otherwise the general items.
-template <int TX, int TY, int K, bool FAST>
+// smaller shared-memory footprint and higher occupancy); otherwise the general
+// items, SPEC: those holding source or port cells (the only ones that compile the
+// source and port-sample code; their own table and launch as well).
+template <int TX, int TY, int K, bool FAST, bool SPEC>
 __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BShape<TX, TY, K>::MINB)
     batch2d_pass(BPass P) {
     using SH = BShape<TX, TY, K>;
@@ -283,8 +285,8 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                 if (r >= 1 && gi >= 1 && gi <= nx - 2 && gj < ny - 1) f |= F_HY;
                 if (r < RX - 1 && c < RY - 1 && gi < nx - 1 && gj < ny - 1) f |= F_EZ;
                 if (r >= K && r < K + TX && c >= K && c < K + TY) f |= F_INT;
-                if (gi == sI.src_x && (unsigned)(gj - sI.src_y0) < (unsigned)sI.src_n) f |= F_SRC;
-                if (f & F_INT)
+                if (SPEC && gi == sI.src_x && (unsigned)(gj - sI.src_y0) < (unsigned)sI.src_n) f |= F_SRC;
+                if (SPEC && (f & F_INT))
                     for (int q = 0; q < sI.nport; ++q)
                         if (gi == sI.mx[q] && (unsigned)(gj - sI.my0[q]) < (unsigned)sI.mn[q]) f |= F_PORT;
                 if (cp) {
@@ -307,7 +309,9 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
         }
         __syncthreads();
 
-#pragma unroll
+        // the step loop stays rolled: K copies of this body (M cells each, with the
+        // CPML, source and port code) overflow the instruction cache
+#pragma unroll 1
         for (int s = 0; s < K; ++s) {
             // H^{n+1/2} from Ez^n
 #pragma unroll
@@ -330,7 +334,7 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
             __syncthreads();
             // Ez^{n+1} from H^{n+1/2}, then the source at t_{n+1} and the port samples
             double amp = 0.0;
-            if (P.live) {
+            if (SPEC && P.live) {
                 const long long n = base + P.s_off + s;
                 if (n < P.namps) amp = P.amps[n];
             }
@@ -347,12 +351,12 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                         if (qy != 255u) c2 = cpml_d(c2, sb[qy], sa[qy], sk[qy], qZY[idx]);
                     }
                     float e = __fmaf_rn(cbr[m], __fsub_rn(c1, c2), sE[idx]);
-                    if (P.live && (f & F_SRC)) {
+                    if (SPEC && P.live && (f & F_SRC)) {
                         const int gj = gy0 + (idx - (idx / RY) * RY);
                         e = __fadd_rn(e, static_cast<float>(P.w[sI.w_off + (gj - sI.src_y0)] * amp));
                     }
                     sE[idx] = e;
-                    if (P.live && P.ring && (f & F_PORT)) {
+                    if (SPEC && P.live && P.ring && (f & F_PORT)) {
                         const int gi = gx0 + idx / RY, gj = gy0 + (idx - (idx / RY) * RY);
                         for (int q = 0; q < sI.nport; ++q)
                             if (gi == sI.mx[q] && (unsigned)(gj - sI.my0[q]) < (unsigned)sI.mn[q])
@@ -395,8 +399,8 @@ __global__ void batch_advance(long long* step, int n) {
 
 struct Variant {
     int tx, ty, k, k1;  // tile, steps per pass, index of the K=1 sibling
-    const void* fn[2];  // [0]: fast-path items, [1]: general items
-    size_t smem[2];
+    const void* fn[3];  // [0]: fast-path items, [1]: general items, [2]: source / port items
+    size_t smem[3];
 };
 
 #define PC_BV(TX, TY, K, K1)                                                                          \
@@ -404,9 +408,10 @@ struct Variant {
      TY,                                                                                              \
      K,                                                                                               \
      K1,                                                                                              \
-     {reinterpret_cast<const void*>(&batch2d_pass<TX, TY, K, true>),                                 \
-      reinterpret_cast<const void*>(&batch2d_pass<TX, TY, K, false>)},                                \
-     {BShape<TX, TY, K>::SMEM_FAST, BShape<TX, TY, K>::SMEM}}
+     {reinterpret_cast<const void*>(&batch2d_pass<TX, TY, K, true, false>),                          \
+      reinterpret_cast<const void*>(&batch2d_pass<TX, TY, K, false, false>),                         \
+      reinterpret_cast<const void*>(&batch2d_pass<TX, TY, K, false, true>)},                          \
+     {BShape<TX, TY, K>::SMEM_FAST, BShape<TX, TY, K>::SMEM, BShape<TX, TY, K>::SMEM}}
 const Variant kVariants[] = {
     PC_BV(32, 64, 1, 0),  PC_BV(32, 64, 2, 0),  PC_BV(32, 64, 4, 0),  PC_BV(32, 64, 8, 0),
     PC_BV(16, 128, 1, 4), PC_BV(16, 128, 2, 4), PC_BV(16, 128, 4, 4), PC_BV(64, 64, 1, 7),
@@ -447,11 +452,11 @@ struct pc_batch {
     int variant = 1;
     int graph_steps = 80;
     int item_variant = -1;
-    int4* d_items = nullptr;  // fast-path items, then general items
+    int4* d_items = nullptr;  // fast-path items, then general items, then source / port items
     int nitems = 0;
-    int nfast = 0;
+    int nfast = 0, ngen = 0;  // fast items, then general ones, then source / port ones
     int items_cap = 0;
-    int grid[kNumVariants][2] = {};
+    int grid[kNumVariants][3] = {};
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int graph_key[2][2] = {{-1, -1}, {-1, -1}};  // (variant, graph_steps) the graph was captured for
@@ -503,17 +508,19 @@ int build_items(pc_batch* b, int v) {
     if (b->d_items) drop_graphs(b);  // captured graphs hold the previous table
     std::vector<int> ord(items.size());
     std::iota(ord.begin(), ord.end(), 0);
-    // fast-path items first, then the general ones; each class longest first
+    // fast-path items first, then the general ones without and then those with
+    // source or port cells; each class longest first
+    auto cls = [&](int a) { return (items[a].w & 2) ? 2 : ((items[a].w & 1) ? 1 : 0); };
     std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) {
-        const bool fa = (items[a].w & 3) == 0, fc = (items[c].w & 3) == 0;
-        if (fa != fc) return fa;
+        if (cls(a) != cls(c)) return cls(a) < cls(c);
         return cost[a] > cost[c];
     });
     std::vector<int4> sorted(items.size());
-    int nfast = 0;
+    int nfast = 0, ngen = 0;
     for (size_t q = 0; q < ord.size(); ++q) {
         sorted[q] = items[ord[q]];
-        nfast += (sorted[q].w & 3) == 0 ? 1 : 0;
+        nfast += cls(ord[q]) == 0 ? 1 : 0;
+        ngen += cls(ord[q]) == 1 ? 1 : 0;
     }
     if ((int)sorted.size() > b->items_cap) {
         cudaFree(b->d_items);
@@ -525,6 +532,7 @@ int build_items(pc_batch* b, int v) {
     PC_CUDA_CHECK(cudaMemcpy(b->d_items, sorted.data(), sorted.size() * sizeof(int4), cudaMemcpyHostToDevice));
     b->nitems = (int)sorted.size();
     b->nfast = nfast;
+    b->ngen = ngen;
     b->item_variant = v;
     return PC_OK;
 }
@@ -578,10 +586,11 @@ BPass make_pass(pc_batch* b, int s_off, int row0, bool live) {
 // the number of kernels launched (or a negative error).
 int launch_pass(pc_batch* b, int v, const BPass& P0, cudaStream_t s) {
     int launched = 0;
-    for (int path = 0; path < 2; ++path) {
+    for (int path = 0; path < 3; ++path) {
         BPass P = P0;
-        P.items = P0.items + (path == 0 ? 0 : b->nfast);
-        P.nitems = path == 0 ? b->nfast : P0.nitems - b->nfast;
+        const int first[3] = {0, b->nfast, b->nfast + b->ngen};
+        P.items = P0.items + first[path];
+        P.nitems = path == 2 ? P0.nitems - first[2] : first[path + 1] - first[path];
         if (P.nitems <= 0) continue;
         const int g = grid_for(b, v, path);
         if (g <= 0) return PC_ERR_CUDA;
