@@ -254,13 +254,157 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
             }
             continue;
         }
-        float cbr[M];
-
-        // ---- general path: per-cell validity, CPML, source and port samples ----
         const int64_t pyx = sI.p_off;                      // psi Hy (x-derivative), [2t][pitch]
         const int64_t pzx = pyx + 2 * (int64_t)t * pitch;  // psi Ez (x-derivative), [2t][pitch]
         const int64_t pxy = pyx + 4 * (int64_t)t * pitch;  // psi Hx (y-derivative), [nx][2t]
         const int64_t pzy = pxy + 2 * (int64_t)t * nx;     // psi Ez (y-derivative), [nx][2t]
+        if (!SPEC) {
+            // ---- CPML path: items at the instance edges or on the CPML slabs, without
+            // source or port cells.  The fast path's y-adjacent pairs and guard cells
+            // (region-edge cells compute garbage that never reaches the shrinking valid
+            // region), plus per-cell flags only where the stencil of the reference
+            // stepper differs: components it does not update at the instance edges keep
+            // their value (a select, so even the sign of a zero is kept), the psi
+            // recursions run on slab cells that update, cells outside the instance load
+            // as zero and are never stored.
+            constexpr int NP = RC / 2;
+            constexpr int MP = (NP + BNT - 1) / BNT;
+            float2 cb2[MP];
+            unsigned fl2[2 * MP];  // per cell: bit 0 Hx, 1 Hy, 2 Ez, 3 interior; x slab << 8, y slab << 16
+#pragma unroll
+            for (int m = 0; m < MP; ++m) {
+                const int q = tid + m * BNT;
+                cb2[m] = make_float2(0.f, 0.f);
+                fl2[2 * m] = fl2[2 * m + 1] = (255u << 8) | (255u << 16);
+                if (q >= NP) continue;
+                const int idx = 2 * q;
+                const int r = idx / RY, c0 = idx - (idx / RY) * RY;
+                const int gi = gx0 + r;
+                float cbv[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int c = c0 + h, gj = gy0 + c;
+                    const bool in = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
+                    float e = 0.f, hx = 0.f, hy = 0.f;
+                    cbv[h] = 0.f;
+                    unsigned f = 0, sxs = 255, sys = 255;
+                    if (in) {
+                        const int64_t o = (int64_t)gi * pitch + gj;
+                        e = fin[o];
+                        hx = fin[nxp + o];
+                        hy = fin[2 * nxp + o];
+                        cbv[h] = cbp[o];
+                        if (gi < nx - 1 && gj >= 1 && gj <= ny - 2) f |= 1u;
+                        if (gi >= 1 && gi <= nx - 2 && gj < ny - 1) f |= 2u;
+                        if (gi < nx - 1 && gj < ny - 1) f |= 4u;
+                        if (r >= K && r < K + TX && c >= K && c < K + TY) f |= 8u;
+                        if (cp) {
+                            sxs = slab_idx(gi, nx, t);
+                            sys = slab_idx(gj, ny, t);
+                            if (sxs != 255) {
+                                qYX[idx + h] = P.psi_in[pyx + (int64_t)sxs * pitch + gj];
+                                qZX[idx + h] = P.psi_in[pzx + (int64_t)sxs * pitch + gj];
+                            }
+                            if (sys != 255) {
+                                qXY[idx + h] = P.psi_in[pxy + (int64_t)gi * (2 * t) + sys];
+                                qZY[idx + h] = P.psi_in[pzy + (int64_t)gi * (2 * t) + sys];
+                            }
+                        }
+                    }
+                    fl2[2 * m + h] = f | (sxs << 8) | (sys << 16);
+                    sE[idx + h] = e;
+                    sX[idx + h] = hx;
+                    sY[idx + h] = hy;
+                }
+                cb2[m] = make_float2(cbv[0], cbv[1]);
+            }
+            __syncthreads();
+#pragma unroll 1
+            for (int s = 0; s < K; ++s) {
+#pragma unroll
+                for (int m = 0; m < MP; ++m) {
+                    const int q = tid + m * BNT;
+                    if (q >= NP) continue;
+                    const int idx = 2 * q;
+                    const float2 e = *reinterpret_cast<const float2*>(sE + idx);
+                    const float2 eu = *reinterpret_cast<const float2*>(sE + idx - RY);
+                    const float em = sE[idx - 1];
+                    float2 hx = *reinterpret_cast<const float2*>(sX + idx);
+                    float2 hy = *reinterpret_cast<const float2*>(sY + idx);
+                    float cy[2] = {diff(e.x, em, idy), diff(e.y, e.x, idy)};
+                    float cx[2] = {diff(e.x, eu.x, idx_), diff(e.y, eu.y, idx_)};
+                    float* hxp = &hx.x;
+                    float* hyp = &hy.x;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const unsigned f = fl2[2 * m + h];
+                        const unsigned qx = (f >> 8) & 255u, qy = (f >> 16) & 255u;
+                        if ((f & 1u) && qy != 255u) cy[h] = cpml_d(cy[h], sb[qy], sa[qy], sk[qy], qXY[idx + h]);
+                        if ((f & 2u) && qx != 255u) cx[h] = cpml_d(cx[h], sb[qx], sa[qx], sk[qx], qYX[idx + h]);
+                        hxp[h] = (f & 1u) ? h_minus(hxp[h], cy[h], da, db) : hxp[h];
+                        hyp[h] = (f & 2u) ? h_plus(hyp[h], cx[h], da, db) : hyp[h];
+                    }
+                    *reinterpret_cast<float2*>(sX + idx) = hx;
+                    *reinterpret_cast<float2*>(sY + idx) = hy;
+                }
+                __syncthreads();
+#pragma unroll
+                for (int m = 0; m < MP; ++m) {
+                    const int q = tid + m * BNT;
+                    if (q >= NP) continue;
+                    const int idx = 2 * q;
+                    const float2 hx = *reinterpret_cast<const float2*>(sX + idx);
+                    const float2 hy = *reinterpret_cast<const float2*>(sY + idx);
+                    const float2 hyd = *reinterpret_cast<const float2*>(sY + idx + RY);
+                    const float hxn = sX[idx + 2];
+                    float2 e = *reinterpret_cast<const float2*>(sE + idx);
+                    float c1[2] = {diff(hyd.x, hy.x, idx_), diff(hyd.y, hy.y, idx_)};
+                    float c2[2] = {diff(hx.y, hx.x, idy), diff(hxn, hx.y, idy)};
+                    float* ep = &e.x;
+                    const float cbv[2] = {cb2[m].x, cb2[m].y};
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const unsigned f = fl2[2 * m + h];
+                        const unsigned qx = (f >> 8) & 255u, qy = (f >> 16) & 255u;
+                        if ((f & 4u) && qx != 255u) c1[h] = cpml_d(c1[h], sb[qx], sa[qx], sk[qx], qZX[idx + h]);
+                        if ((f & 4u) && qy != 255u) c2[h] = cpml_d(c2[h], sb[qy], sa[qy], sk[qy], qZY[idx + h]);
+                        ep[h] = (f & 4u) ? __fmaf_rn(cbv[h], __fsub_rn(c1[h], c2[h]), ep[h]) : ep[h];
+                    }
+                    *reinterpret_cast<float2*>(sE + idx) = e;
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int m = 0; m < MP; ++m) {
+                const int q = tid + m * BNT;
+                if (q >= NP) continue;
+                const int idx = 2 * q;
+                const int gi = gx0 + idx / RY;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const unsigned f = fl2[2 * m + h];
+                    if (!(f & 8u)) continue;
+                    const int gj = gy0 + (idx + h - (idx / RY) * RY);
+                    const int64_t o = (int64_t)gi * pitch + gj;
+                    fout[o] = sE[idx + h];
+                    fout[nxp + o] = sX[idx + h];
+                    fout[2 * nxp + o] = sY[idx + h];
+                    const unsigned qx = (f >> 8) & 255u, qy = (f >> 16) & 255u;
+                    if (qx != 255u) {
+                        P.psi_out[pyx + (int64_t)qx * pitch + gj] = qYX[idx + h];
+                        P.psi_out[pzx + (int64_t)qx * pitch + gj] = qZX[idx + h];
+                    }
+                    if (qy != 255u) {
+                        P.psi_out[pxy + (int64_t)gi * (2 * t) + qy] = qXY[idx + h];
+                        P.psi_out[pzy + (int64_t)gi * (2 * t) + qy] = qZY[idx + h];
+                    }
+                }
+            }
+            continue;
+        }
+        float cbr[M];
+
+        // ---- general path: per-cell validity, CPML, source and port samples ----
         unsigned fl[M];
 #pragma unroll
         for (int m = 0; m < M; ++m) {
