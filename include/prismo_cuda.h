@@ -165,6 +165,24 @@ int pc_add_dft(pc_ctx* ctx, int32_t comp, const int64_t* offsets, int32_t npts, 
                int32_t nf, double dt, double t0, void* d_acc);
 int pc_dft_flush(pc_ctx* ctx, int32_t id, void* stream);
 
+/* Flux monitor, time domain (monitors/flux.py:110-173 FluxMonitor.update and
+ * _compute_power_flow): after every step (after the DFT samples)
+ *   d_hist[n] = scale * sum_p (F0 F1 - F2 F3)(p)
+ * with F0..F3 the components comps[0..3] at offsets[q * npts + p] (for a plane
+ * normal to x: Ey, Hz, Ez, Hy and scale = dy dz), n counting the steps since the
+ * monitor was added; steps beyond `capacity` are counted, not stored.  d_hist is
+ * caller-owned float64 [capacity].  Returns the monitor id. */
+int pc_add_flux(pc_ctx* ctx, const int32_t comps[4], const int64_t* offsets, int32_t npts, double scale,
+                double* d_hist, int64_t capacity);
+/* Steps sampled so far by flux monitor `id` (synchronises the stream). */
+int pc_flux_count(pc_ctx* ctx, int32_t id, int64_t* count, void* stream);
+/* Flux monitor, frequency domain (monitors/flux.py:219-285
+ * get_frequency_domain_power): flushes the four DFT monitors dft_ids (same points
+ * and frequencies, components F0..F3 as above) and writes
+ *   d_out[f] = scale / 2 * sum_p Re(F0 F1* - F2 F3*)
+ * for every frequency (device float64 [nf]). */
+int pc_flux_spectrum(pc_ctx* ctx, const int32_t dft_ids[4], double scale, double* d_out, void* stream);
+
 /* Read and clear the device status word (PC_STATUS_* bits). Synchronises the
  * stream. */
 int pc_status(pc_ctx* ctx, uint32_t* flags, void* stream);

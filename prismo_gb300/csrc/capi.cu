@@ -147,6 +147,7 @@ void pc_destroy(pc_ctx* c) {
         cudaFree(s.d_w);
     }
     for (auto& m : c->dfts) dft_monitor_free(m);
+    for (auto& m : c->fluxes) flux_monitor_free(m);
     cudaFree(c->d_amps);
     cudaFree(c->d_cpml_coef);
     cudaFree(c->d_cpml_slab);
@@ -346,6 +347,10 @@ int one_step(pc_ctx* c, int n, const double* tamp, cudaStream_t s) {
     if (rc) return rc;
     if (!c->dfts.empty()) {
         rc = dft_after_step(c, s);
+        if (rc) return rc;
+    }
+    if (!c->fluxes.empty()) {
+        rc = flux_after_step(c, s);
         if (rc) return rc;
     }
     return PC_OK;

@@ -1,0 +1,161 @@
+// Flux monitors: power through a plane, in time and in frequency.
+//
+// monitors/flux.py:126-173 sums S_n = (E x H)_n over the monitor surface times the
+// cell area every step, and :219-285 forms P(w) = 1/2 Re sum (E x H*)_n dA from
+// the DFTs of the fields; both take the field values at the same index for every
+// component.  The reference's region is a fixed [:10, :10] placeholder
+// (flux.py:104-106, 187-191); here the plane is the monitor's real region, the
+// components' common index range.
+//
+// Time domain: one CTA per plane after every step gathers the four tangential
+// components, reduces in float64 and appends to the history at a device counter
+// (so a replayed graph of steps appends in order).  Frequency domain: the four
+// components' DFT monitors (dft.cu) are flushed and one CTA per frequency reduces
+// their accumulators.
+#include "pc_internal.cuh"
+
+namespace pc {
+namespace {
+
+constexpr int FLUX_THREADS = 256;
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    v = threadIdx.x < FLUX_THREADS / 32 ? sh[threadIdx.x] : 0.0;
+    if (warp == 0)
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(FLUX_THREADS) flux_sample(const T* f0, const T* f1, const T* f2, const T* f3,
+                                                           const int64_t* __restrict__ off, int npts, double scale,
+                                                           double* hist, int64_t* count, int64_t capacity) {
+    __shared__ double sh[FLUX_THREADS / 32];
+    double acc = 0.0;
+    for (int p = threadIdx.x; p < npts; p += FLUX_THREADS) {
+        const double a = (double)f0[off[p]] * (double)f1[off[npts + p]];
+        const double b = (double)f2[off[2 * npts + p]] * (double)f3[off[3 * npts + p]];
+        acc += a - b;
+    }
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) {
+        const int64_t n = *count;
+        if (n < capacity) hist[n] = acc * scale;
+        *count = n + 1;
+    }
+}
+
+// P(f) = 1/2 Re sum_p (A B* - C D*) * scale from four DFT accumulators
+// (float4: running sum re, im and their Kahan compensations).
+__global__ void __launch_bounds__(FLUX_THREADS) flux_spectrum(const float4* a, const float4* b, const float4* c,
+                                                             const float4* d, int npts, double scale, double* out) {
+    __shared__ double sh[FLUX_THREADS / 32];
+    const int f = blockIdx.x;
+    auto val = [&](const float4* x, int p, double& re, double& im) {
+        const float4 v = x[(int64_t)f * npts + p];
+        re = (double)v.x - (double)v.z;
+        im = (double)v.y - (double)v.w;
+    };
+    double acc = 0.0;
+    for (int p = threadIdx.x; p < npts; p += FLUX_THREADS) {
+        double ar, ai, br, bi, cr, ci, dr, di;
+        val(a, p, ar, ai);
+        val(b, p, br, bi);
+        val(c, p, cr, ci);
+        val(d, p, dr, di);
+        acc += (ar * br + ai * bi) - (cr * dr + ci * di);  // Re(A B*) - Re(C D*)
+    }
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) out[f] = 0.5 * acc * scale;
+}
+
+}  // namespace
+
+int flux_after_step(pc_ctx* c, cudaStream_t s) {
+    for (auto& m : c->fluxes) {
+        const int64_t n = m.npts;
+        if (c->g.precision == 8) {
+            auto F = [&](int q) { return static_cast<const double*>(c->F[c->cur][m.comp[q]]); };
+            flux_sample<double><<<1, FLUX_THREADS, 0, s>>>(F(0), F(1), F(2), F(3), m.d_off, (int)n, m.scale,
+                                                           m.d_hist, m.d_count, m.capacity);
+        } else {
+            auto F = [&](int q) { return static_cast<const float*>(c->F[c->cur][m.comp[q]]); };
+            flux_sample<float><<<1, FLUX_THREADS, 0, s>>>(F(0), F(1), F(2), F(3), m.d_off, (int)n, m.scale,
+                                                          m.d_hist, m.d_count, m.capacity);
+        }
+        ++c->launches;
+    }
+    PC_CUDA_CHECK(cudaGetLastError());
+    return PC_OK;
+}
+
+void flux_monitor_free(FluxMonitor& m) {
+    cudaFree(m.d_off);
+    cudaFree(m.d_count);
+    m.d_off = nullptr;
+    m.d_count = nullptr;
+}
+
+}  // namespace pc
+
+using namespace pc;
+
+int pc_add_flux(pc_ctx* c, const int32_t comps[4], const int64_t* offsets, int32_t npts, double scale, double* d_hist,
+                int64_t capacity) {
+    if (c) ++c->gen;  // captured time loops are stale
+    if (!c || !comps || !offsets || npts <= 0 || !d_hist || capacity <= 0) return PC_ERR_INVALID;
+    for (int q = 0; q < 4; ++q)
+        if (comps[q] < 0 || comps[q] > 5) return PC_ERR_INVALID;
+    const int64_t limit = (int64_t)c->g.nx * c->g.ny * c->g.pitch;
+    for (int64_t i = 0; i < 4 * (int64_t)npts; ++i)
+        if (offsets[i] < 0 || offsets[i] >= limit) return PC_ERR_INVALID;
+    FluxMonitor m{};
+    for (int q = 0; q < 4; ++q) m.comp[q] = comps[q];
+    m.npts = npts;
+    m.scale = scale;
+    m.d_hist = d_hist;
+    m.capacity = capacity;
+    bool ok = cudaMalloc(&m.d_off, 4 * (size_t)npts * sizeof(int64_t)) == cudaSuccess &&
+              cudaMalloc(&m.d_count, sizeof(int64_t)) == cudaSuccess;
+    ok = ok && cudaMemcpy(m.d_off, offsets, 4 * (size_t)npts * sizeof(int64_t), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemset(m.d_count, 0, sizeof(int64_t)) == cudaSuccess;
+    if (!ok) {
+        flux_monitor_free(m);
+        return PC_ERR_CUDA;
+    }
+    c->fluxes.push_back(m);
+    return (int)c->fluxes.size() - 1;
+}
+
+int pc_flux_count(pc_ctx* c, int32_t id, int64_t* count, void* stream) {
+    if (!c || !count || id < 0 || id >= (int)c->fluxes.size()) return PC_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    PC_CUDA_CHECK(cudaMemcpyAsync(count, c->fluxes[id].d_count, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    PC_CUDA_CHECK(cudaStreamSynchronize(s));
+    return PC_OK;
+}
+
+int pc_flux_spectrum(pc_ctx* c, const int32_t dft_ids[4], double scale, double* d_out, void* stream) {
+    if (!c || !dft_ids || !d_out) return PC_ERR_INVALID;
+    const int nd = (int)c->dfts.size();
+    for (int q = 0; q < 4; ++q)
+        if (dft_ids[q] < 0 || dft_ids[q] >= nd) return PC_ERR_INVALID;
+    const DftMonitor& m0 = c->dfts[dft_ids[0]];
+    for (int q = 1; q < 4; ++q)
+        if (c->dfts[dft_ids[q]].npts != m0.npts || c->dfts[dft_ids[q]].nf != m0.nf) return PC_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int q = 0; q < 4; ++q) {
+        const int rc = dft_flush_monitor(c, c->dfts[dft_ids[q]], s);
+        if (rc) return rc;
+    }
+    flux_spectrum<<<m0.nf, FLUX_THREADS, 0, s>>>(c->dfts[dft_ids[0]].d_acc, c->dfts[dft_ids[1]].d_acc,
+                                                 c->dfts[dft_ids[2]].d_acc, c->dfts[dft_ids[3]].d_acc, m0.npts, scale,
+                                                 d_out);
+    ++c->launches;
+    PC_CUDA_CHECK(cudaGetLastError());
+    return PC_OK;
+}

@@ -39,6 +39,18 @@ struct DftMonitor {
     float4* d_acc;    // [nf][npts] (sum re, sum im, comp re, comp im), caller-owned
 };
 
+// Flux plane: per step, sum over its points of (F0 F1 - F2 F3) times `scale`
+// (the normal Poynting component of the tangential fields times the cell area)
+// appended to a float64 history at a device counter.
+struct FluxMonitor {
+    int comp[4], npts;
+    double scale;
+    int64_t* d_off;     // [4][npts] element offsets (ctx-owned)
+    int64_t* d_count;   // steps sampled so far (ctx-owned)
+    double* d_hist;     // [capacity], caller-owned
+    int64_t capacity;
+};
+
 #define PC_MAX_ADE_REGIONS 2
 #define PC_MAX_ADE_POLES 4
 
@@ -137,6 +149,7 @@ struct pc_ctx {
     // sources and DFT monitors
     std::vector<pc::SourceDesc> sources;
     std::vector<pc::DftMonitor> dfts;
+    std::vector<pc::FluxMonitor> fluxes;
     double* d_amps;
     size_t amps_cap;
     std::vector<double> amps_host;  // repacked source columns when a TFSF column is present
@@ -190,6 +203,8 @@ int dft_monitor_init(DftMonitor& m, int comp, const int64_t* offsets, int npts, 
                      double t0, void* d_acc, int64_t limit);
 void dft_monitor_free(DftMonitor& m);
 int dft_flush_monitor(pc_ctx* c, DftMonitor& m, cudaStream_t s);
+int flux_after_step(pc_ctx* c, cudaStream_t s);
+void flux_monitor_free(FluxMonitor& m);
 
 }  // namespace pc
 

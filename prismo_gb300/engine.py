@@ -128,6 +128,7 @@ class FDTDEngine:
             self._set_cpml(pml)
         self.sources = []  # (comp, offsets, weights, waveform)
         self.dfts = []  # (comp, offsets, omegas, accumulator tensor)
+        self.fluxes = []  # per-step power histories (device float64)
         self._closed = False
 
     # -- setup ---------------------------------------------------------------
@@ -321,6 +322,39 @@ class FDTDEngine:
         _lib.check(self.lib.pc_dft_flush(self.ctx, int(mid), self._stream_ptr()), "pc_dft_flush")
         acc = self.dfts[mid][3].double()
         return torch_complex(acc[..., 0] - acc[..., 2], acc[..., 1] - acc[..., 3])
+
+    # -- flux monitors -----------------------------------------------------------
+    def add_flux(self, comps, offsets, scale: float, capacity: int = 1 << 18) -> int:
+        """Per-step power sum_p (F0 F1 - F2 F3)(p) * scale through a plane, F0..F3
+        the components ``comps`` at ``offsets`` [4][npts]; returns the monitor id."""
+        torch = _torch()
+        offs = np.ascontiguousarray(offsets, dtype=np.int64).reshape(4, -1)
+        cs = (C.c_int32 * 4)(*[COMP_INDEX[c] for c in comps])
+        hist = torch.zeros(int(capacity), dtype=torch.float64, device=self.device)
+        fid = _lib.check(self.lib.pc_add_flux(self.ctx, cs, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                                              int(offs.shape[1]), float(scale), hist.data_ptr(), int(capacity)),
+                         "pc_add_flux")
+        self.fluxes.append(hist)
+        return fid
+
+    def flux_history(self, fid: int) -> np.ndarray:
+        """Power of every step sampled so far by flux monitor ``fid`` (float64)."""
+        n = C.c_int64(0)
+        _lib.check(self.lib.pc_flux_count(self.ctx, int(fid), C.byref(n), self._stream_ptr()), "pc_flux_count")
+        hist = self.fluxes[fid]
+        if n.value > hist.numel():
+            raise RuntimeError(f"flux monitor {fid}: {n.value} steps sampled, history holds {hist.numel()}")
+        return hist[:n.value].cpu().numpy()
+
+    def flux_spectrum(self, dft_ids, scale: float) -> np.ndarray:
+        """1/2 Re sum_p (F0 F1* - F2 F3*) * scale from the DFT monitors ``dft_ids``."""
+        torch = _torch()
+        nf = self.dfts[dft_ids[0]][2].size
+        out = torch.zeros(nf, dtype=torch.float64, device=self.device)
+        ids = (C.c_int32 * 4)(*[int(i) for i in dft_ids])
+        _lib.check(self.lib.pc_flux_spectrum(self.ctx, ids, float(scale), out.data_ptr(), self._stream_ptr()),
+                   "pc_flux_spectrum")
+        return out.cpu().numpy()
 
     # -- stepping --------------------------------------------------------------
     def step(self, nsteps: int = 1, amps: Optional[np.ndarray] = None):

@@ -168,3 +168,114 @@ class DFTMonitor(FieldMonitor):
         if normalize and spec.max() > 0:
             spec = spec / spec.max()
         return spec
+
+
+class FluxMonitor(Monitor):
+    """monitors/flux.py:18-330: power through a plane normal to x, y or z.
+
+    Time domain: after every step, sum over the plane of the normal Poynting
+    component of the instantaneous fields times the cell area (flux.py:126-173);
+    frequency domain: P(w) = 1/2 Re sum (E x H*)_n dA from the DFTs of the
+    tangential fields (flux.py:219-285).  As in the reference every component is
+    taken at the same index (no interpolation between staggered positions).  The
+    plane is the monitor's region (the components' common index range) instead of
+    the reference's fixed [:10, :10] placeholder (flux.py:104-106, 187-191), and
+    on a 2D grid the area element counts one metre along z (power per unit length;
+    the reference's 2D spacing has dz = 0, core/grid.py:105).  On
+    the cuda engine both are computed on the device (flux.cu), the time-domain
+    history into a device buffer of ``capacity`` steps."""
+
+    # (F0, F1, F2, F3) with S_n = F0 F1 - F2 F3 (flux.py:148-150)
+    _TERMS = {"x": ("Ey", "Hz", "Ez", "Hy"), "y": ("Ez", "Hx", "Ex", "Hz"), "z": ("Ex", "Hy", "Ey", "Hx")}
+
+    def __init__(self, center, size, direction, name: Optional[str] = None, frequencies=None, backend=None,
+                 capacity: int = 1 << 18):
+        super().__init__(center, size, name)
+        self.direction = direction.lower()
+        if self.direction not in ("x", "y", "z"):
+            raise ValueError("direction must be 'x', 'y', or 'z'")
+        self._power_flow_history: list = []
+        self._time_history: list = []
+        self.frequencies = frequencies
+        if frequencies is not None:
+            self.omega = 2 * np.pi * np.array(frequencies)
+        self.eps0 = 8.854187817e-12
+        self.mu0 = 4 * np.pi * 1e-7
+        self.capacity = int(capacity)
+        self._engine = None
+        self._fid = None
+        self._dft_ids = None
+        self._host_dft = None
+        self._t0 = self._dt = None
+
+    def initialize(self, grid) -> None:
+        super().initialize(grid)
+        terms = self._TERMS[self.direction]
+        common = [min(len(np.asarray(self._monitor_region[c][a]).ravel()) for c in terms)
+                  for a in range(len(self._monitor_region[terms[0]]))]
+        self._plane = {}
+        for c in terms:
+            ax = [np.asarray(self._monitor_region[c][a]).ravel()[:common[a]] for a in range(len(common))]
+            self._plane[c] = np.ix_(*ax)
+        dx, dy, dz = grid.spacing
+        if dz == 0:  # 2D: power per metre along the invariant z (the reference's dz = 0 makes it zero)
+            dz = 1.0
+        self._dA = {"x": dy * dz, "y": dx * dz, "z": dx * dy}[self.direction]
+        self._power_flow_history = []
+        self._time_history = []
+        if self.frequencies is not None:
+            self._host_dft = {c: np.zeros((len(self.frequencies),) + tuple(np.broadcast_shapes(
+                *(a.shape for a in self._plane[c]))), dtype=np.complex128) for c in terms}
+
+    def attach(self, engine, t0: float) -> None:
+        terms = self._TERMS[self.direction]
+        offs = np.stack([engine.offsets(c, self._plane[c]) for c in terms])
+        self._engine, self._t0, self._dt = engine, t0, engine.dt
+        self._fid = engine.add_flux(terms, offs, self._dA, self.capacity)
+        if self.frequencies is not None:
+            self._dft_ids = [engine.add_dft(c, offs[q], self.frequencies, t0) for q, c in enumerate(terms)]
+
+    @property
+    def device_sampled(self) -> bool:
+        """True when the engine samples this monitor inside its steps."""
+        return self._engine is not None
+
+    def update(self, fields, time: float, dt: float) -> None:
+        if self._engine is not None:  # sampled on the device every step
+            return
+        a, b, c, d = (fields[k][self._plane[k]] for k in self._TERMS[self.direction])
+        to = (lambda x: x.to_numpy()) if hasattr(a, "to_numpy") else np.asarray
+        a, b, c, d = to(a), to(b), to(c), to(d)
+        self._power_flow_history.append(float(np.sum(a * b - c * d) * self._dA))
+        self._time_history.append(time)
+        if self.frequencies is not None:
+            for fi, w in enumerate(self.omega):
+                ph = np.exp(-1j * w * time) * dt
+                for k, x in zip(self._TERMS[self.direction], (a, b, c, d)):
+                    self._host_dft[k][fi] += x * ph
+
+    def get_time_domain_power(self):
+        """(time array, power array) of every step since the monitor was added."""
+        if self._engine is not None:
+            p = self._engine.flux_history(self._fid)
+            return self._t0 + self._dt * np.arange(p.size), p
+        return np.array(self._time_history), np.array(self._power_flow_history)
+
+    def get_frequency_domain_power(self, frequency_index: Optional[int] = None):
+        if self.frequencies is None:
+            raise RuntimeError("No frequencies specified for this monitor")
+        if self._engine is not None:
+            p = self._engine.flux_spectrum(self._dft_ids, self._dA)
+        else:
+            a, b, c, d = (self._host_dft[k] for k in self._TERMS[self.direction])
+            p = np.array([0.5 * np.real(np.sum(a[i] * np.conj(b[i]) - c[i] * np.conj(d[i]))) * self._dA
+                          for i in range(len(self.frequencies))])
+        return p if frequency_index is None else float(p[frequency_index])
+
+    def get_transmission(self, reference_power=None):
+        if self.frequencies is not None:
+            power = self.get_frequency_domain_power()
+        else:
+            _, hist = self.get_time_domain_power()
+            power = np.mean(hist) if len(hist) > 0 else 0.0
+        return power / reference_power if reference_power is not None else power

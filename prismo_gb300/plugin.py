@@ -174,13 +174,18 @@ def _adapt_monitor(mon):
                            components=list(mon.components), name=mon.name)
         _mirror(mon, out)
         return out
+    if name == "FluxMonitor":
+        out = M.FluxMonitor(center=mon.center, size=mon.size, direction=mon.direction, name=mon.name,
+                            frequencies=None if mon.frequencies is None else list(mon.frequencies))
+        _mirror(mon, out)
+        return out
     raise TypeError(f"monitor type {name} is not supported by the cuda backend")
 
 
 def _mirror(ref, native):
     """Route the reference monitor's accessors to the device monitor."""
     for attr in ("get_time_data", "get_frequency_data", "get_power_flow", "get_intensity", "get_power_spectrum",
-                 "update", "initialize"):
+                 "get_time_domain_power", "get_frequency_domain_power", "get_transmission", "update", "initialize"):
         if hasattr(native, attr):
             setattr(ref, attr, getattr(native, attr))
     ref._native = native

@@ -111,7 +111,8 @@ class Simulation:
 
     def _needs_host_each_step(self) -> bool:
         return bool(self._host_sources) or any(
-            not isinstance(m, FieldMonitor) or m.time_domain or m._engine is None for m in self.monitors)
+            not getattr(m, "device_sampled", False) and (not isinstance(m, FieldMonitor) or m.time_domain or
+                                                         m._engine is None) for m in self.monitors)
 
     def step(self) -> None:
         """core/simulation.py:147-164."""

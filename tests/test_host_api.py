@@ -128,3 +128,45 @@ def test_gaussian_beam_and_mode_sources_host_side():
     a = amplitude_table([ms], t)[:, 0]
     np.testing.assert_allclose(a, 2.0 * np.array([wf(x) for x in t]) * np.cos(0.3 - 2 * np.pi * 193e12 * t),
                                rtol=1e-14, atol=1e-300)
+
+
+def test_flux_monitor_interface_and_host_path():
+    """FluxMonitor as the reference's tests construct it (tests/test_monitors_advanced.py
+    TestFluxMonitor), and its host path (fields given on the host, no engine)
+    against the flux.py:126-173 / 219-285 formulas evaluated directly."""
+    from prismo_gb300 import FluxMonitor
+    from prismo_gb300.grid import GridSpec, YeeGrid
+
+    m = FluxMonitor(center=(0, 0, 0), size=(0, 1e-6, 0), direction="x", frequencies=[193e12])
+    assert m.direction == "x" and m.frequencies is not None
+    with pytest.raises(ValueError):
+        FluxMonitor(center=(0, 0, 0), size=(0, 1e-6, 0), direction="w")
+    grid = YeeGrid(GridSpec(size=(5e-6, 3e-6, 0), resolution=10e6))
+    m = FluxMonitor(center=(0, 0, 0), size=(0, 1e-6, 0), direction="x")
+    m.initialize(grid)
+    assert m._power_flow_history == [] and m._time_history == []
+
+    grid = YeeGrid(GridSpec(size=(1e-6, 0.8e-6, 0.6e-6), resolution=20e6))
+    freqs = [180e12, 200e12]
+    m = FluxMonitor(center=(0.5e-6, 0.4e-6, 0.3e-6), size=(0.5e-6, 0.0, 0.3e-6), direction="y", frequencies=freqs)
+    m.initialize(grid)
+    rng = np.random.default_rng(3)
+    dt = 1e-17
+    want = []
+    dft = {c: 0 for c in m._TERMS["y"]}
+    for n in range(5):
+        fields = {c: rng.standard_normal(grid.get_field_shape(c)) for c in O.COMPONENTS}
+        t = (n + 1) * dt
+        m.update(fields, t, dt)
+        a, b, c, d = (fields[k][m._plane[k]] for k in m._TERMS["y"])
+        want.append(np.sum(a * b - c * d) * grid.dx * grid.dz)
+        for k in m._TERMS["y"]:
+            dft[k] = dft[k] + np.stack([fields[k][m._plane[k]] * np.exp(-2j * np.pi * f * t) * dt for f in freqs])
+    t, p = m.get_time_domain_power()
+    np.testing.assert_allclose(p, want, rtol=1e-12)
+    np.testing.assert_allclose(t, dt * np.arange(1, 6))
+    A, B, C, D = (dft[k] for k in m._TERMS["y"])
+    spec = [0.5 * np.real(np.sum(A[i] * np.conj(B[i]) - C[i] * np.conj(D[i]))) * grid.dx * grid.dz
+            for i in range(len(freqs))]
+    np.testing.assert_allclose(m.get_frequency_domain_power(), spec, rtol=1e-12)
+    assert m._plane["Ez"][1].ravel().size == 1  # a plane normal to y
