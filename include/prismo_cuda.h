@@ -183,6 +183,23 @@ int pc_flux_count(pc_ctx* ctx, int32_t id, int64_t* count, void* stream);
  * for every frequency (device float64 [nf]). */
 int pc_flux_spectrum(pc_ctx* ctx, const int32_t dft_ids[4], double scale, double* d_out, void* stream);
 
+/* Mode-expansion monitor (monitors/mode_monitor.py:137-199 with
+ * utils/mode_matching.py:41-131): after every step, for every mode m
+ *   d_hist[n][m] = sum_{q<4, p<npts} w[m][q][p] * F_q(offsets[q * npts + p])
+ * (complex weights, float64 (re, im) pairs [nmodes][4][npts]; the host folds the
+ * mode profile, the cross-product signs and 1 / (2 P_m) into them), n counting
+ * the steps since the monitor was added.  d_hist is caller-owned complex128
+ * [capacity][nmodes]; nmodes <= 64.  Returns the monitor id. */
+int pc_add_mode_monitor(pc_ctx* ctx, const int32_t comps[4], const int64_t* offsets, int32_t npts, int32_t nmodes,
+                        const double* weights, void* d_hist, int64_t capacity);
+int pc_mode_count(pc_ctx* ctx, int32_t id, int64_t* count, void* stream);
+/* d_out[m][f] = sum_n d_hist[n][m] exp(-i omega_f (t0 + n dt)) dt over the steps
+ * sampled so far (mode_monitor.py:171-175; t0 = time of the first sample);
+ * omega is a host array; synchronises the stream.  PC_ERR_STATE when more steps
+ * were sampled than the history holds. */
+int pc_mode_spectrum(pc_ctx* ctx, int32_t id, const double* omega, int32_t nf, double t0, double dt, void* d_out,
+                     void* stream);
+
 /* Read and clear the device status word (PC_STATUS_* bits). Synchronises the
  * stream. */
 int pc_status(pc_ctx* ctx, uint32_t* flags, void* stream);

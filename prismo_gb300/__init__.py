@@ -34,6 +34,6 @@ from .materials import (  # noqa: F401,E402
     LorentzMaterial,
     LorentzPole,
 )
-from .monitors import DFTMonitor, FieldMonitor, FluxMonitor, Monitor  # noqa: F401,E402
+from .monitors import DFTMonitor, FieldMonitor, FluxMonitor, ModeExpansionMonitor, Monitor  # noqa: F401,E402
 from .simulation import Simulation  # noqa: F401,E402
 from .solver import FDTDSolver, MaxwellUpdater  # noqa: F401,E402

@@ -124,6 +124,11 @@ SIGNATURES = {
                               C.c_void_p, C.c_int64]),
     "pc_flux_count": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.c_void_p]),
     "pc_flux_spectrum": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_double, C.c_void_p, C.c_void_p]),
+    "pc_add_mode_monitor": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.c_int32, C.c_int32,
+                                      C.POINTER(C.c_double), C.c_void_p, C.c_int64]),
+    "pc_mode_count": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.c_void_p]),
+    "pc_mode_spectrum": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int32, C.c_double, C.c_double,
+                                   C.c_void_p, C.c_void_p]),
     "pc_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p]),
     "pc_launch_count": (C.c_int64, [C.c_void_p]),
     "pc_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64]),

@@ -148,6 +148,7 @@ void pc_destroy(pc_ctx* c) {
     }
     for (auto& m : c->dfts) dft_monitor_free(m);
     for (auto& m : c->fluxes) flux_monitor_free(m);
+    for (auto& m : c->modes) mode_monitor_free(m);
     cudaFree(c->d_amps);
     cudaFree(c->d_cpml_coef);
     cudaFree(c->d_cpml_slab);
@@ -351,6 +352,10 @@ int one_step(pc_ctx* c, int n, const double* tamp, cudaStream_t s) {
     }
     if (!c->fluxes.empty()) {
         rc = flux_after_step(c, s);
+        if (rc) return rc;
+    }
+    if (!c->modes.empty()) {
+        rc = mode_after_step(c, s);
         if (rc) return rc;
     }
     return PC_OK;

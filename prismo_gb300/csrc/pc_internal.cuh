@@ -51,6 +51,20 @@ struct FluxMonitor {
     int64_t capacity;
 };
 
+// Mode-expansion plane: per step and mode m, a_m = sum over c, p of w[m][c][p]
+// F_c(p) (complex weights from the mode profile) appended to a complex history
+// [capacity][nmodes] at a device counter.
+struct ModeMonitor {
+    int comp[4], npts, nmodes;
+    int64_t* d_off;     // [4][npts] (ctx-owned)
+    double2* d_w;       // [nmodes][4][npts] (ctx-owned)
+    int64_t* d_count;   // (ctx-owned)
+    double2* d_hist;    // [capacity][nmodes], caller-owned
+    int64_t capacity;
+    double* d_omega;    // spectrum scratch (ctx-owned)
+    int omega_cap;
+};
+
 #define PC_MAX_ADE_REGIONS 2
 #define PC_MAX_ADE_POLES 4
 
@@ -150,6 +164,7 @@ struct pc_ctx {
     std::vector<pc::SourceDesc> sources;
     std::vector<pc::DftMonitor> dfts;
     std::vector<pc::FluxMonitor> fluxes;
+    std::vector<pc::ModeMonitor> modes;
     double* d_amps;
     size_t amps_cap;
     std::vector<double> amps_host;  // repacked source columns when a TFSF column is present
@@ -205,6 +220,8 @@ void dft_monitor_free(DftMonitor& m);
 int dft_flush_monitor(pc_ctx* c, DftMonitor& m, cudaStream_t s);
 int flux_after_step(pc_ctx* c, cudaStream_t s);
 void flux_monitor_free(FluxMonitor& m);
+int mode_after_step(pc_ctx* c, cudaStream_t s);
+void mode_monitor_free(ModeMonitor& m);
 
 }  // namespace pc
 

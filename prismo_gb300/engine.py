@@ -129,6 +129,7 @@ class FDTDEngine:
         self.sources = []  # (comp, offsets, weights, waveform)
         self.dfts = []  # (comp, offsets, omegas, accumulator tensor)
         self.fluxes = []  # per-step power histories (device float64)
+        self.mode_mons = []  # per-step mode-coefficient histories (device complex128)
         self._closed = False
 
     # -- setup ---------------------------------------------------------------
@@ -354,6 +355,43 @@ class FDTDEngine:
         ids = (C.c_int32 * 4)(*[int(i) for i in dft_ids])
         _lib.check(self.lib.pc_flux_spectrum(self.ctx, ids, float(scale), out.data_ptr(), self._stream_ptr()),
                    "pc_flux_spectrum")
+        return out.cpu().numpy()
+
+    # -- mode-expansion monitors ------------------------------------------------
+    def add_mode_monitor(self, comps, offsets, weights, capacity: int = 1 << 16) -> int:
+        """Per-step complex a_m = sum_q,p weights[m][q][p] F_q(offsets[q][p]) for every
+        mode m (weights complex [nmodes][4][npts]); returns the monitor id."""
+        torch = _torch()
+        offs = np.ascontiguousarray(offsets, dtype=np.int64).reshape(4, -1)
+        w = np.asarray(weights, dtype=np.complex128)
+        nm = w.shape[0]
+        wr = np.ascontiguousarray(np.stack([w.real, w.imag], axis=-1).reshape(-1))
+        cs = (C.c_int32 * 4)(*[COMP_INDEX[c] for c in comps])
+        hist = torch.zeros((int(capacity), nm), dtype=torch.complex128, device=self.device)
+        mid = _lib.check(self.lib.pc_add_mode_monitor(
+            self.ctx, cs, offs.ctypes.data_as(C.POINTER(C.c_int64)), int(offs.shape[1]), int(nm),
+            wr.ctypes.data_as(C.POINTER(C.c_double)), hist.data_ptr(), int(capacity)), "pc_add_mode_monitor")
+        self.mode_mons.append(hist)
+        return mid
+
+    def mode_history(self, mid: int) -> np.ndarray:
+        """[steps][nmodes] complex coefficients sampled so far."""
+        n = C.c_int64(0)
+        _lib.check(self.lib.pc_mode_count(self.ctx, int(mid), C.byref(n), self._stream_ptr()), "pc_mode_count")
+        hist = self.mode_mons[mid]
+        if n.value > hist.shape[0]:
+            raise RuntimeError(f"mode monitor {mid}: {n.value} steps sampled, history holds {hist.shape[0]}")
+        return hist[:n.value].cpu().numpy()
+
+    def mode_spectrum(self, mid: int, freqs, t0: float) -> np.ndarray:
+        """[nmodes][nf] sum_n a_m(t_n) exp(-i w t_n) dt, t_n = t0 + n dt."""
+        torch = _torch()
+        om = np.ascontiguousarray(2 * np.pi * np.asarray(freqs, dtype=np.float64))
+        nm = self.mode_mons[mid].shape[1]
+        out = torch.zeros((nm, om.size), dtype=torch.complex128, device=self.device)
+        _lib.check(self.lib.pc_mode_spectrum(self.ctx, int(mid), om.ctypes.data_as(C.POINTER(C.c_double)),
+                                             int(om.size), float(t0), float(self.dt), out.data_ptr(),
+                                             self._stream_ptr()), "pc_mode_spectrum")
         return out.cpu().numpy()
 
     # -- stepping --------------------------------------------------------------

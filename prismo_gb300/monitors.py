@@ -279,3 +279,159 @@ class FluxMonitor(Monitor):
             _, hist = self.get_time_domain_power()
             power = np.mean(hist) if len(hist) > 0 else 0.0
         return power / reference_power if reference_power is not None else power
+
+
+def _resize_linear(a: np.ndarray, shape) -> np.ndarray:
+    """A mode profile resized to the plane by first-order spline zoom, as
+    utils/mode_matching.py:442-472 resizes it."""
+    a = np.asarray(a)
+    if a.shape == tuple(shape):
+        return a
+    from scipy.ndimage import zoom
+
+    f = tuple(t / s for t, s in zip(shape, a.shape))
+    if np.iscomplexobj(a):
+        return zoom(a.real, f, order=1) + 1j * zoom(a.imag, f, order=1)
+    return zoom(a, f, order=1)
+
+
+class ModeExpansionMonitor(Monitor):
+    """monitors/mode_monitor.py:19-400: waveguide-mode coefficients on a plane.
+
+    Every step, for every mode m (utils/mode_matching.py:41-131, with the unit
+    spacing the reference monitor passes, mode_monitor.py:176-178):
+        a_m = 1/2 sum_plane (E x H_m* + E_m* x H)_n / P_m,
+        P_m = |1/2 Re sum_mode (E_m x H_m*)_n|
+    (the simulation fields are real, so E_m* x H needs no conjugate of H); the
+    frequency spectrum accumulates a_m exp(-i w t) dt (mode_monitor.py:171-175).
+    The plane is the monitor's region (the tangential components' common index
+    range; the reference extracts a fixed [:10, :10] placeholder,
+    mode_monitor.py:222-226); mode arrays of another shape are resized to it as
+    the reference resizes them.  On the cuda engine the coefficients are reduced on
+    the device every step (flux.cu) into a history of ``capacity`` steps.  ``modes``
+    are objects with Ex, Ey, Ez, Hx, Hy, Hz arrays (modes/solver.py:17-60)."""
+
+    _TERMS = FluxMonitor._TERMS
+
+    def __init__(self, center, size, modes, direction: str = "x", frequencies=None, name: Optional[str] = None,
+                 backend=None, capacity: int = 1 << 16):
+        super().__init__(center, size, name)
+        self.modes = list(modes)
+        self.direction = direction.lower()
+        self.frequencies = frequencies
+        if self.direction not in ("x", "y", "z"):
+            raise ValueError("direction must be 'x', 'y', or 'z'")
+        self._mode_coeffs_time = {i: [] for i in range(len(self.modes))}
+        self._time_points: list = []
+        if frequencies is not None:
+            self.omega = 2 * np.pi * np.array(frequencies)
+            self._mode_coeffs_freq = {i: np.zeros(len(frequencies), dtype=complex) for i in range(len(self.modes))}
+        self.capacity = int(capacity)
+        self._engine = None
+        self._mid = None
+        self._t0 = None
+
+    def initialize(self, grid) -> None:
+        super().initialize(grid)
+        terms = self._TERMS[self.direction]
+        common = [min(len(np.asarray(self._monitor_region[c][a]).ravel()) for c in terms)
+                  for a in range(len(self._monitor_region[terms[0]]))]
+        self._plane = {c: np.ix_(*[np.asarray(self._monitor_region[c][a]).ravel()[:common[a]]
+                                   for a in range(len(common))]) for c in terms}
+        full = tuple(common)
+        squeezed = tuple(n for n in full if n != 1) or (1,)
+        self._weights = np.zeros((len(self.modes), 4) + full, dtype=np.complex128)
+        self._mode_norms = np.ones(len(self.modes))
+        f0, f1, f2, f3 = terms  # S_n = F0 F1 - F2 F3: E_a H_b - E_c H_d
+        for m, mode in enumerate(self.modes):
+            md = {c: np.asarray(getattr(mode, c)) for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")}
+            s = md[f0] * np.conj(md[f1]) - md[f2] * np.conj(md[f3])
+            p = abs(0.5 * np.real(np.sum(s)))
+            self._mode_norms[m] = p
+            if p <= 1e-20:  # compute_mode_overlap returns 0 for a powerless mode
+                continue
+            r = {c: (md[c].reshape(full) if md[c].size == int(np.prod(full)) else
+                     _resize_linear(np.squeeze(md[c]), squeezed).reshape(full)) for c in md}
+            k = 0.5 / p
+            # E_sim x H_m*: F0 conj(H_m[f1]) - F2 conj(H_m[f3]); E_m* x H_sim: E_m[f0] F1 - E_m[f2] F3
+            self._weights[m, 0] = k * np.conj(r[f1])
+            self._weights[m, 1] = k * r[f0]
+            self._weights[m, 2] = -k * np.conj(r[f3])
+            self._weights[m, 3] = -k * r[f2]
+
+    def attach(self, engine, t0: float) -> None:
+        terms = self._TERMS[self.direction]
+        offs = np.stack([engine.offsets(c, self._plane[c]) for c in terms])
+        w = self._weights.reshape(len(self.modes), 4, -1)
+        self._engine, self._t0 = engine, t0
+        self._mid = engine.add_mode_monitor(terms, offs, w, self.capacity)
+
+    @property
+    def device_sampled(self) -> bool:
+        return self._engine is not None
+
+    def update(self, fields, time: float, dt: float) -> None:
+        if self._engine is not None:  # sampled on the device every step
+            return
+        terms = self._TERMS[self.direction]
+        vals = []
+        for c in terms:
+            x = fields[c][self._plane[c]]
+            vals.append(x.to_numpy() if hasattr(x, "to_numpy") else np.asarray(x))
+        for m in range(len(self.modes)):
+            a = complex(sum(np.sum(self._weights[m, q] * vals[q]) for q in range(4)))
+            self._mode_coeffs_time[m].append(a)
+            if self.frequencies is not None:
+                self._mode_coeffs_freq[m] += a * np.exp(-1j * self.omega * time) * dt
+        self._time_points.append(time)
+
+    def _sync(self):
+        if self._engine is None:
+            return
+        h = self._engine.mode_history(self._mid)
+        self._mode_coeffs_time = {m: list(h[:, m]) for m in range(len(self.modes))}
+        self._time_points = list(self._t0 + self._engine.dt * np.arange(h.shape[0]))
+        if self.frequencies is not None:
+            spec = self._engine.mode_spectrum(self._mid, self.frequencies, self._t0)
+            self._mode_coeffs_freq = {m: spec[m] for m in range(len(self.modes))}
+
+    def get_mode_coefficient(self, mode_index: int, domain: str = "time"):
+        self._sync()
+        if domain == "time":
+            return self._mode_coeffs_time[mode_index]
+        if domain == "frequency":
+            if self.frequencies is None:
+                raise RuntimeError("No frequencies specified")
+            return self._mode_coeffs_freq[mode_index]
+        raise ValueError("domain must be 'time' or 'frequency'")
+
+    def separate_forward_backward(self, mode_index: int, frequency_index: int):
+        if self.frequencies is None:
+            raise RuntimeError("Frequency-domain decomposition required")
+        self._sync()
+        return self._mode_coeffs_freq[mode_index][frequency_index], 0.0
+
+    def get_mode_power(self, mode_index: int, frequency_index: Optional[int] = None):
+        self._sync()
+        if frequency_index is not None:
+            return float(np.abs(self._mode_coeffs_freq[mode_index][frequency_index]) ** 2)
+        return np.mean(np.abs(np.array(self._mode_coeffs_time[mode_index])) ** 2)
+
+    def get_mode_transmission(self, mode_index: int, reference_power: Optional[float] = None):
+        if self.frequencies is None:
+            raise RuntimeError("Frequency-domain analysis required")
+        self._sync()
+        power = np.abs(self._mode_coeffs_freq[mode_index]) ** 2
+        if reference_power is not None:
+            return power / reference_power
+        return power / np.max(power) if np.max(power) > 0 else power
+
+    def compute_s_parameters(self, source_mode_index: int = 0, source_power: float = 1.0):
+        if self.frequencies is None:
+            raise RuntimeError("Frequency-domain analysis required")
+        self._sync()
+        out = {}
+        for m in range(len(self.modes)):
+            c = self._mode_coeffs_freq[m]
+            out[f"S_{m + 1}{source_mode_index + 1}"] = c / np.sqrt(source_power) if source_power > 0 else c
+        return out

@@ -174,6 +174,12 @@ def _adapt_monitor(mon):
                            components=list(mon.components), name=mon.name)
         _mirror(mon, out)
         return out
+    if name == "ModeExpansionMonitor":
+        out = M.ModeExpansionMonitor(center=mon.center, size=mon.size, modes=list(mon.modes), direction=mon.direction,
+                                     frequencies=None if mon.frequencies is None else list(mon.frequencies),
+                                     name=mon.name)
+        _mirror(mon, out)
+        return out
     if name == "FluxMonitor":
         out = M.FluxMonitor(center=mon.center, size=mon.size, direction=mon.direction, name=mon.name,
                             frequencies=None if mon.frequencies is None else list(mon.frequencies))
@@ -185,7 +191,9 @@ def _adapt_monitor(mon):
 def _mirror(ref, native):
     """Route the reference monitor's accessors to the device monitor."""
     for attr in ("get_time_data", "get_frequency_data", "get_power_flow", "get_intensity", "get_power_spectrum",
-                 "get_time_domain_power", "get_frequency_domain_power", "get_transmission", "update", "initialize"):
+                 "get_time_domain_power", "get_frequency_domain_power", "get_transmission", "get_mode_coefficient",
+                 "separate_forward_backward", "get_mode_power", "get_mode_transmission", "compute_s_parameters",
+                 "update", "initialize"):
         if hasattr(native, attr):
             setattr(ref, attr, getattr(native, attr))
     ref._native = native

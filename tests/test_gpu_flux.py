@@ -88,3 +88,48 @@ def test_flux_monitor_3d_fused_matches_oracle(pg):
     assert rel(p, hist) <= 1e-4, rel(p, hist)
     assert rel(mon.get_frequency_domain_power(), spec) <= 1e-4
     assert sim.check() == 0
+
+
+def test_mode_expansion_monitor_matches_oracle(pg):
+    """ModeExpansionMonitor on the device: per-step coefficients and spectra of two
+    modes on a 2D x plane against the same weights (pinned to the reference's
+    compute_mode_overlap in test_host_api.py) applied to the oracle's fields."""
+    from types import SimpleNamespace
+
+    size = ((60 - 8 - 0.5) * 20e-9, (50 - 8 - 0.5) * 20e-9, 0.0)
+    sim = pg.Simulation(size=size, resolution=1 / 20e-9, pml_layers=4, courant_factor=0.5)
+    src = pg.ElectricDipole(position=(0.3e-6, 0.4e-6, 0.0), polarization="z", frequency=193e12, pulse_width=4e-15)
+    sim.add_source(src)
+    rng = np.random.default_rng(7)
+    probe = pg.ModeExpansionMonitor(center=(0.6e-6, 0.4e-6, 0.0), size=(0.0, 0.5e-6, 0.0), modes=[])
+    probe.initialize(sim.grid)
+    npts = probe._plane["Ez"][1].size
+    y = np.linspace(-1, 1, 2 * npts + 3)  # another length: resized to the plane as the reference does
+    modes = [SimpleNamespace(Ex=0 * y, Ey=0 * y, Ez=np.exp(-4 * y**2) * (1 + 0.3j * k), Hx=0 * y,
+                             Hy=-np.exp(-4 * y**2) / 377.0 * (1 - 0.2j * k), Hz=0 * y) for k in range(2)]
+    freqs = [185e12, 193e12, 205e12]
+    mon = pg.ModeExpansionMonitor(center=(0.6e-6, 0.4e-6, 0.0), size=(0.0, 0.5e-6, 0.0), modes=modes,
+                                  direction="x", frequencies=freqs)
+    sim.add_monitor(mon)
+    n = 250
+    sim.run(n * sim.dt * (1 - 1e-12))
+    g = O.OracleGrid(size, 1 / 20e-9, 4)
+    o = O.OracleFDTD(g, g.suggest_dt(0.5), cpml_layers=4)
+    o.add_source("Ez", src._source_region["Ez"], O.gaussian_pulse(193e12, 4e-15))
+    terms = mon._TERMS["x"]
+    want = []
+    for _ in range(n):
+        o.step()
+        vals = [o.F[c][mon._plane[c]] for c in terms]
+        want.append([sum(np.sum(mon._weights[m, q] * vals[q]) for q in range(4)) for m in range(2)])
+    want = np.array(want)
+    t = sim.dt * np.arange(1, n + 1)
+    for m in range(2):
+        got = np.array(mon.get_mode_coefficient(m))
+        assert np.abs(want[:, m]).max() > 0
+        assert rel(got, want[:, m]) <= 1e-4, rel(got, want[:, m])
+        spec = [np.sum(want[:, m] * np.exp(-2j * np.pi * f * t)) * sim.dt for f in freqs]
+        assert rel(mon.get_mode_coefficient(m, "frequency"), spec) <= 1e-4
+    assert mon.get_mode_power(0, 1) == pytest.approx(abs(mon.get_mode_coefficient(0, "frequency")[1]) ** 2)
+    assert set(mon.compute_s_parameters()) == {"S_11", "S_21"}
+    assert sim.check() == 0

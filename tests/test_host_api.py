@@ -170,3 +170,64 @@ def test_flux_monitor_interface_and_host_path():
             for i in range(len(freqs))]
     np.testing.assert_allclose(m.get_frequency_domain_power(), spec, rtol=1e-12)
     assert m._plane["Ez"][1].ravel().size == 1  # a plane normal to y
+
+
+def _reference_mode_matching():
+    """utils/mode_matching.py of the reference when its source tree is present."""
+    import importlib.util
+
+    for root in (os.environ.get("PRISMO_REFERENCE_SRC", ""), "/root/reference/src"):
+        p = os.path.join(root, "prismo", "utils", "mode_matching.py") if root else ""
+        if p and os.path.exists(p):
+            import sys
+            import types
+
+            for name in ("prismo", "prismo.modes", "prismo.modes.solver"):
+                sys.modules.setdefault(name, types.ModuleType(name))
+            sys.modules["prismo.modes.solver"].WaveguideMode = object
+            spec = importlib.util.spec_from_file_location("_ref_mode_matching", p)
+            mod = importlib.util.module_from_spec(spec)
+            spec.loader.exec_module(mod)
+            return mod
+    return None
+
+
+def test_mode_expansion_monitor_host_path_matches_reference_overlap():
+    """ModeExpansionMonitor's per-step coefficients (host path) against the
+    reference's own compute_mode_overlap (utils/mode_matching.py:41-131, unit
+    spacing as mode_monitor.py:176-178 passes) on the same plane arrays, and its
+    spectrum against the mode_monitor.py:171-175 accumulation."""
+    from types import SimpleNamespace
+
+    from prismo_gb300 import ModeExpansionMonitor
+    from prismo_gb300.grid import GridSpec, YeeGrid
+
+    mm = _reference_mode_matching()
+    if mm is None:
+        pytest.skip("reference source tree not present")
+    grid = YeeGrid(GridSpec(size=(1e-6, 0.8e-6, 0.6e-6), resolution=20e6))
+    rng = np.random.default_rng(5)
+    mon = ModeExpansionMonitor(center=(0.5e-6, 0.4e-6, 0.3e-6), size=(0.0, 0.5e-6, 0.3e-6), modes=[],
+                               direction="x", frequencies=[190e12, 200e12])
+    mon.initialize(grid)
+    shp = tuple(np.broadcast_shapes(*(a.shape for a in mon._plane["Ey"])))
+    modes = [SimpleNamespace(**{c: rng.standard_normal(shp) + 1j * rng.standard_normal(shp)
+                                for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")}) for _ in range(2)]
+    mon = ModeExpansionMonitor(center=(0.5e-6, 0.4e-6, 0.3e-6), size=(0.0, 0.5e-6, 0.3e-6), modes=modes,
+                               direction="x", frequencies=[190e12, 200e12])
+    mon.initialize(grid)
+    dt = 1e-17
+    want = [[], []]
+    for n in range(4):
+        fields = {c: rng.standard_normal(grid.get_field_shape(c)) for c in O.COMPONENTS}
+        mon.update(fields, (n + 1) * dt, dt)
+        sim = {c: fields[c][mon._plane[c]] if c in mon._plane else np.zeros(shp)
+               for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")}
+        for m, mode in enumerate(modes):
+            want[m].append(mm.compute_mode_overlap(sim["Ex"], sim["Ey"], sim["Ez"], sim["Hx"], sim["Hy"], sim["Hz"],
+                                                   mode, direction="x", dx=1.0, dy=1.0))
+    for m in range(2):
+        np.testing.assert_allclose(mon.get_mode_coefficient(m), want[m], rtol=1e-12)
+        t = dt * np.arange(1, 5)
+        spec = [np.sum(np.array(want[m]) * np.exp(-1j * w * t) * dt) for w in mon.omega]
+        np.testing.assert_allclose(mon.get_mode_coefficient(m, "frequency"), spec, rtol=1e-12)
