@@ -182,12 +182,23 @@ def _reference_mode_matching():
             import sys
             import types
 
-            for name in ("prismo", "prismo.modes", "prismo.modes.solver"):
-                sys.modules.setdefault(name, types.ModuleType(name))
-            sys.modules["prismo.modes.solver"].WaveguideMode = object
-            spec = importlib.util.spec_from_file_location("_ref_mode_matching", p)
-            mod = importlib.util.module_from_spec(spec)
-            spec.loader.exec_module(mod)
+            # the module imports prismo.modes.solver.WaveguideMode for type hints only:
+            # stand-ins while it loads, then the import table as it was
+            names = ("prismo", "prismo.modes", "prismo.modes.solver")
+            saved = {n: sys.modules.get(n) for n in names}
+            try:
+                for n in names:
+                    sys.modules[n] = types.ModuleType(n)
+                sys.modules["prismo.modes.solver"].WaveguideMode = object
+                spec = importlib.util.spec_from_file_location("_ref_mode_matching", p)
+                mod = importlib.util.module_from_spec(spec)
+                spec.loader.exec_module(mod)
+            finally:
+                for n, m in saved.items():
+                    if m is None:
+                        sys.modules.pop(n, None)
+                    else:
+                        sys.modules[n] = m
             return mod
     return None
 
