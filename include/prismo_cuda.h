@@ -200,6 +200,20 @@ int pc_mode_count(pc_ctx* ctx, int32_t id, int64_t* count, void* stream);
 int pc_mode_spectrum(pc_ctx* ctx, int32_t id, const double* omega, int32_t nf, double t0, double dt, void* d_out,
                      void* stream);
 
+/* Anisotropic field update (materials/tensor.py:437-590 AnisotropicUpdater),
+ * elementwise over n cells of same-shaped device arrays (precision 4 or 8):
+ *   sign +1 (E):  out = F + scale * curl / diag            (diagonal)
+ *                 out = F + scale * (M . curl)              (full, M row-major)
+ *   sign -1 (H):  out = F - scale * curl / diag, out = F + (-scale) * (M . curl)
+ * with scale = dt/eps0 or dt/mu0, the coefficients per cell (device d_coef
+ * [3 or 9][n] in the array precision) or uniform (host coef_uniform [3 or 9],
+ * used when d_coef is null); M is the inverse tensor.  Rounded in the
+ * reference's evaluation order (float64 equals NumPy bit for bit).  out may
+ * alias fields. */
+int pc_aniso_update(int32_t precision, int32_t diagonal, int32_t sign, const void* const fields[3],
+                    const void* const curls[3], void* const out[3], int64_t n, const void* d_coef,
+                    const double* coef_uniform, double scale, void* stream);
+
 /* Read and clear the device status word (PC_STATUS_* bits). Synchronises the
  * stream. */
 int pc_status(pc_ctx* ctx, uint32_t* flags, void* stream);

@@ -124,6 +124,9 @@ SIGNATURES = {
                               C.c_void_p, C.c_int64]),
     "pc_flux_count": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.c_void_p]),
     "pc_flux_spectrum": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_double, C.c_void_p, C.c_void_p]),
+    "pc_aniso_update": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                  C.POINTER(C.c_void_p), C.c_int64, C.c_void_p, C.POINTER(C.c_double), C.c_double,
+                                  C.c_void_p]),
     "pc_add_mode_monitor": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.c_int32, C.c_int32,
                                       C.POINTER(C.c_double), C.c_void_p, C.c_int64]),
     "pc_mode_count": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.c_void_p]),

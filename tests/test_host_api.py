@@ -242,3 +242,25 @@ def test_mode_expansion_monitor_host_path_matches_reference_overlap():
         t = dt * np.arange(1, 5)
         spec = [np.sum(np.array(want[m]) * np.exp(-1j * w * t) * dt) for w in mon.omega]
         np.testing.assert_allclose(mon.get_mode_coefficient(m, "frequency"), spec, rtol=1e-12)
+
+
+def test_tensor_material_matches_reference_inverses():
+    """prismo_gb300.tensor containers against the reference's TensorMaterial
+    (materials/tensor.py:110-312): full matrices, diagonal test, inverses."""
+    from prismo_gb300.tensor import TensorComponents, TensorMaterial
+    from test_plugin import SOURCE_TREES, _import_reference
+
+    _import_reference(SOURCE_TREES)
+    from prismo.materials import tensor as RT
+
+    rng = np.random.default_rng(2)
+    cases = [dict(xx=2.0, yy=3.0, zz=4.0), dict(xx=2.2, yy=2.5, zz=3.1, xy=0.3, xz=-0.2, yz=0.1, yx=0.25),
+             dict(xx=rng.uniform(2, 4, (3, 4)), yy=rng.uniform(2, 4, (3, 4)), zz=rng.uniform(2, 4, (3, 4)),
+                  xy=rng.uniform(-0.3, 0.3, (3, 4)))]
+    for kw in cases:
+        ours = TensorMaterial(TensorComponents(**kw))
+        ref = RT.TensorMaterial(RT.TensorComponents(**kw))
+        assert ours.is_diagonal == ref.is_diagonal
+        np.testing.assert_array_equal(ours.epsilon_tensor, np.asarray(ref.epsilon_tensor))
+        np.testing.assert_allclose(ours.get_inverse_epsilon(), ref.get_inverse_epsilon(), rtol=1e-14, atol=1e-15)
+        np.testing.assert_allclose(ours.get_inverse_mu(), ref.get_inverse_mu(), rtol=1e-14)
