@@ -200,6 +200,18 @@ int pc_mode_count(pc_ctx* ctx, int32_t id, int64_t* count, void* stream);
 int pc_mode_spectrum(pc_ctx* ctx, int32_t id, const double* omega, int32_t nf, double t0, double dt, void* d_out,
                      void* stream);
 
+/* Mode ports (boundaries/mode_port.py:261-429), on device arrays outside a
+ * context.  pc_scatter_add: field[off[i]] = field[off[i]] + amp * w[i] computed in
+ * float64 and rounded once to the field type (precision 4 or 8); d_off (int64
+ * element offsets) and d_w (float64) are device arrays of n entries.
+ * pc_plane_overlap: d_out[m] = sum_{q<4, p<npts} w[m][q][p] F_q(off[q*npts + p])
+ * for m < nmodes, complex float64 weights [nmodes][4][npts] and output
+ * [nmodes] (re, im) on the device. */
+int pc_scatter_add(int32_t precision, void* field, const int64_t* d_off, const double* d_w, int64_t n, double amp,
+                   void* stream);
+int pc_plane_overlap(int32_t precision, const void* const fields[4], const int64_t* d_off, int32_t npts,
+                     int32_t nmodes, const void* d_w, void* d_out, void* stream);
+
 /* Anisotropic field update (materials/tensor.py:437-590 AnisotropicUpdater),
  * elementwise over n cells of same-shaped device arrays (precision 4 or 8):
  *   sign +1 (E):  out = F + scale * curl / diag            (diagonal)

@@ -37,5 +37,6 @@ from .materials import (  # noqa: F401,E402
 from .monitors import DFTMonitor, FieldMonitor, FluxMonitor, ModeExpansionMonitor, Monitor  # noqa: F401,E402
 from . import export  # noqa: F401,E402
 from .tensor import AnisotropicUpdater, TensorComponents, TensorMaterial  # noqa: F401,E402
+from .ports import ModePort, ModePortConfig  # noqa: F401,E402
 from .simulation import Simulation  # noqa: F401,E402
 from .solver import FDTDSolver, MaxwellUpdater  # noqa: F401,E402

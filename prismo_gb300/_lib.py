@@ -127,6 +127,10 @@ SIGNATURES = {
     "pc_aniso_update": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                   C.POINTER(C.c_void_p), C.c_int64, C.c_void_p, C.POINTER(C.c_double), C.c_double,
                                   C.c_void_p]),
+    "pc_scatter_add": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_double,
+                                 C.c_void_p]),
+    "pc_plane_overlap": (C.c_int, [C.c_int32, C.POINTER(C.c_void_p), C.c_void_p, C.c_int32, C.c_int32, C.c_void_p,
+                                   C.c_void_p, C.c_void_p]),
     "pc_add_mode_monitor": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.c_int32, C.c_int32,
                                       C.POINTER(C.c_double), C.c_void_p, C.c_int64]),
     "pc_mode_count": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.c_void_p]),

@@ -108,6 +108,41 @@ __global__ void __launch_bounds__(FLUX_THREADS) mode_sample(const T* f0, const T
     if (threadIdx.x == 0) *count = n + 1;
 }
 
+// Mode ports (boundaries/mode_port.py:261-429): F[off[p]] += amp w[p] in float64,
+// rounded once to the field type (NumPy's in-place add of a float64 product), and
+// a one-shot complex weighted sum over the port plane for the extraction.
+template <typename T>
+__global__ void scatter_add(T* f, const int64_t* __restrict__ off, const double* __restrict__ w, int64_t n,
+                            double amp) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        f[off[i]] = (T)__dadd_rn((double)f[off[i]], __dmul_rn(amp, w[i]));  // no contraction into an FMA
+}
+
+template <typename T>
+__global__ void __launch_bounds__(FLUX_THREADS) plane_overlap(const T* f0, const T* f1, const T* f2, const T* f3,
+                                                             const int64_t* __restrict__ off,
+                                                             const double2* __restrict__ w, int npts, int nmodes,
+                                                             double2* out) {
+    __shared__ double sh[FLUX_THREADS / 32];
+    const int m = blockIdx.x;
+    const double2* wm = w + (int64_t)m * 4 * npts;
+    double re = 0.0, im = 0.0;
+    for (int p = threadIdx.x; p < npts; p += FLUX_THREADS) {
+        const double v[4] = {(double)f0[off[p]], (double)f1[off[npts + p]], (double)f2[off[2 * npts + p]],
+                             (double)f3[off[3 * npts + p]]};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double2 a = wm[(int64_t)q * npts + p];
+            re += a.x * v[q];
+            im += a.y * v[q];
+        }
+    }
+    re = block_sum(re, sh);
+    __syncthreads();
+    im = block_sum(im, sh);
+    if (threadIdx.x == 0 && m < nmodes) out[m] = make_double2(re, im);
+}
+
 // out[m][f] = sum_{n < nsteps} hist[n][m] exp(-i w_f (t0 + n dt)) dt
 __global__ void __launch_bounds__(FLUX_THREADS) mode_spectrum(const double2* __restrict__ hist, int64_t nsteps,
                                                              int nmodes, const double* __restrict__ omega, int nf,
@@ -304,5 +339,40 @@ int pc_mode_spectrum(pc_ctx* c, int32_t id, const double* omega, int32_t nf, dou
     ++c->launches;
     PC_CUDA_CHECK(cudaGetLastError());
     PC_CUDA_CHECK(cudaStreamSynchronize(s));  // the omega copy's host buffer is the caller's
+    return PC_OK;
+}
+
+int pc_scatter_add(int32_t precision, void* field, const int64_t* d_off, const double* d_w, int64_t n, double amp,
+                   void* stream) {
+    if ((precision != 4 && precision != 8) || !field || !d_off || !d_w || n < 0) return PC_ERR_INVALID;
+    if (n == 0) return PC_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, 1024);
+    if (precision == 8)
+        scatter_add<double><<<blocks, 256, 0, s>>>(static_cast<double*>(field), d_off, d_w, n, amp);
+    else
+        scatter_add<float><<<blocks, 256, 0, s>>>(static_cast<float*>(field), d_off, d_w, n, amp);
+    PC_CUDA_CHECK(cudaGetLastError());
+    return PC_OK;
+}
+
+int pc_plane_overlap(int32_t precision, const void* const fields[4], const int64_t* d_off, int32_t npts,
+                     int32_t nmodes, const void* d_w, void* d_out, void* stream) {
+    if ((precision != 4 && precision != 8) || !fields || !d_off || !d_w || !d_out || npts <= 0 || nmodes <= 0)
+        return PC_ERR_INVALID;
+    for (int q = 0; q < 4; ++q)
+        if (!fields[q]) return PC_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    const double2* w = static_cast<const double2*>(d_w);
+    double2* out = static_cast<double2*>(d_out);
+    if (precision == 8)
+        plane_overlap<double><<<nmodes, FLUX_THREADS, 0, s>>>(
+            static_cast<const double*>(fields[0]), static_cast<const double*>(fields[1]),
+            static_cast<const double*>(fields[2]), static_cast<const double*>(fields[3]), d_off, w, npts, nmodes, out);
+    else
+        plane_overlap<float><<<nmodes, FLUX_THREADS, 0, s>>>(
+            static_cast<const float*>(fields[0]), static_cast<const float*>(fields[1]),
+            static_cast<const float*>(fields[2]), static_cast<const float*>(fields[3]), d_off, w, npts, nmodes, out);
+    PC_CUDA_CHECK(cudaGetLastError());
     return PC_OK;
 }

@@ -264,3 +264,50 @@ def test_tensor_material_matches_reference_inverses():
         np.testing.assert_array_equal(ours.epsilon_tensor, np.asarray(ref.epsilon_tensor))
         np.testing.assert_allclose(ours.get_inverse_epsilon(), ref.get_inverse_epsilon(), rtol=1e-14, atol=1e-15)
         np.testing.assert_allclose(ours.get_inverse_mu(), ref.get_inverse_mu(), rtol=1e-14)
+
+
+def _port_modes(rng, n=2):
+    """Synthetic waveguide modes on their own (x, y) grid (modes/solver.py:17-53 fields)."""
+    from types import SimpleNamespace
+
+    u = np.linspace(0.1e-6, 0.9e-6, 23)
+    v = np.linspace(0.05e-6, 0.7e-6, 17)
+    U, V = np.meshgrid(u, v, indexing="ij")
+    out = []
+    for k in range(n):
+        g = np.exp(-((U - 0.5e-6) ** 2 + (V - 0.35e-6) ** 2) / (0.15e-6) ** 2)
+        f = {c: g * (rng.uniform(0.5, 1.5) + 1j * rng.uniform(-0.5, 0.5)) for c in ("Ex", "Ey", "Ez")}
+        f.update({c: g * (rng.uniform(-0.01, 0.01) + 1j * rng.uniform(-0.01, 0.01)) for c in ("Hx", "Hy", "Hz")})
+        out.append(SimpleNamespace(mode_number=k, neff=2.4 - 0.1 * k, frequency=193e12 + 5e12 * k,
+                                   wavelength=299792458.0 / (193e12 + 5e12 * k), x=u, y=v, power=1.0, **f))
+    return out
+
+
+def test_mode_port_region_and_interpolation_match_reference():
+    """ModePort's plane bounds and interpolated profiles against the reference's
+    own ModePort (boundaries/mode_port.py:112-259) on the same grid and modes."""
+    from prismo_gb300.grid import GridSpec, YeeGrid
+    from prismo_gb300.ports import ModePort, ModePortConfig
+    from test_plugin import SOURCE_TREES, _import_reference
+
+    _import_reference(SOURCE_TREES)
+    from prismo.boundaries import mode_port as RP
+    from prismo.core.grid import GridSpec as RGridSpec
+    from prismo.core.grid import YeeGrid as RYeeGrid
+    from prismo.modes.solver import WaveguideMode
+
+    rng = np.random.default_rng(4)
+    modes = _port_modes(rng)
+    rmodes = [WaveguideMode(**vars(m)) for m in modes]
+    spec = dict(size=(1.2e-6, 1.0e-6, 0.8e-6), resolution=20e6)
+    for direction, center, size in (("+x", (0.5e-6, 0.5e-6, 0.4e-6), (0.0, 0.6e-6, 0.5e-6)),
+                                    ("-y", (0.6e-6, 0.45e-6, 0.4e-6), (0.7e-6, 0.0, 0.5e-6)),
+                                    ("+z", (0.6e-6, 0.5e-6, 0.3e-6), (0.7e-6, 0.6e-6, 0.0))):
+        ours = ModePort(ModePortConfig(center, size, direction, modes, inject=True))
+        ours.initialize(YeeGrid(GridSpec(**spec)))
+        ref = RP.ModePort(RP.ModePortConfig(center, size, direction, rmodes, inject=True))
+        ref.initialize(RYeeGrid(RGridSpec(**spec)))
+        assert ours._port_region == ref._port_region
+        for a, b in zip(ours._interpolated_modes, ref._interpolated_modes):
+            for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz"):
+                np.testing.assert_array_equal(getattr(a, c), getattr(b, c))
