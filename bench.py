@@ -483,11 +483,14 @@ def run_2d(args):
     eng.synchronize()
     n0 = eng.launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(0)
+    clocks.start()
     ev0.record(eng.stream)
     for _ in range(args.steps):
         one()
     ev1.record(eng.stream)
     torch.cuda.synchronize()
+    clk = clocks.stop()
     ms = ev0.elapsed_time(ev1) / args.steps
     cells = float(np.prod(g.dimensions))
     # CPU baseline: the float64 oracle, 50 steps of the same grid, 1 thread
@@ -508,7 +511,7 @@ def run_2d(args):
                   "time_steps_per_s": n / (ms / 1e3), "l2": "grid fits L2 (launch/latency bound)"},
           cpu_baseline={"value": cells / cpu_s / 1e9, "unit": "Gcell/s", "cores": 1, "kind": "port",
                         "sample": f"50 of 3000 steps, float64 oracle, {cpu_s * 1e3:.1f} ms/step"},
-          gpu_launches=eng.launch_count() - n0)
+          gpu_launches=eng.launch_count() - n0, clocks=clk)
     eng.close()
 
 
@@ -580,9 +583,13 @@ def run_sweep(args, cpu, peak, peak_kind):
     cells = sum(I.eps.shape[0] * I.eps.shape[1] for I in B.instances)
     B.close()
     runs = []
+    clocks = ClockSampler(0)
     for q in range(max(args.warmup, 3) + args.steps):
+        if q == max(args.warmup, 3):
+            clocks.start()
         r = S.batched_sweep(designs, layouts=layouts, variant=variant)
         runs.append(r)
+    clk = clocks.stop()
     timed = runs[-args.steps:]
     run_s = sum(r.run_seconds for r in timed) / args.steps
     e2e_s = sum(r.seconds for r in timed) / args.steps
@@ -609,7 +616,7 @@ def run_sweep(args, cpu, peak, peak_kind):
           roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                     "peak_kind": peak_kind, "traffic": None, "bytes_per_cell_update": bpc,
                     "kernel": f"batch2d_pass<{tile[0]},{tile[1]},{tile[2]}> (unblocked bytes; K steps per pass)"},
-          cpu_baseline=cpu, gpu_launches=timed[-1].launches)
+          cpu_baseline=cpu, gpu_launches=timed[-1].launches, clocks=clk)
 
 
 def run_surrogate(args, cpu):
