@@ -93,7 +93,7 @@ struct BShape {
     // general path: two CTAs per SM (64 registers a thread) while the per-cell
     // registers fit; fast path: three CTAs per SM (42 registers) while its pairs fit
     static constexpr int MINB = M <= 8 ? 2 : 1;
-    static constexpr int MINB_FAST = MP <= 4 ? 3 : (MP <= 8 ? 2 : 1);
+    static constexpr int MINB_FAST = MP <= 2 ? 3 : (MP <= 8 ? 2 : 1);
     // Ez, Hx, Hy with RY + 2 guard cells on both sides (the fast path reads
     // neighbours of edge cells without tests), then (general path only) the four
     // CPML auxiliaries
@@ -168,29 +168,31 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
             // of y-adjacent cells and moves them as float2.
             constexpr int NP = RC / 2;
             constexpr int MP = (NP + BNT - 1) / BNT;
-            float2 cb2[MP];
+            // this thread's pairs stay in registers across the K steps; shared memory
+            // carries only what neighbouring threads read
+            float2 cb2[MP], er[MP], xr[MP], yr[MP];
 #pragma unroll
             for (int m = 0; m < MP; ++m) {
                 const int q = tid + m * BNT;
-                cb2[m] = make_float2(0.f, 0.f);
+                cb2[m] = er[m] = xr[m] = yr[m] = make_float2(0.f, 0.f);
                 if (q >= NP) continue;
                 const int idx = 2 * q;
                 const int r = idx / RY, c = idx - (idx / RY) * RY;
                 const int64_t o = (int64_t)(gx0 + r) * pitch + (gy0 + c);
                 if (K % 2 == 0) {  // o is even: 8-byte aligned pairs
-                    *reinterpret_cast<float2*>(sE + idx) = *reinterpret_cast<const float2*>(fin + o);
-                    *reinterpret_cast<float2*>(sX + idx) = *reinterpret_cast<const float2*>(fin + nxp + o);
-                    *reinterpret_cast<float2*>(sY + idx) = *reinterpret_cast<const float2*>(fin + 2 * nxp + o);
+                    er[m] = *reinterpret_cast<const float2*>(fin + o);
+                    xr[m] = *reinterpret_cast<const float2*>(fin + nxp + o);
+                    yr[m] = *reinterpret_cast<const float2*>(fin + 2 * nxp + o);
                     cb2[m] = *reinterpret_cast<const float2*>(cbp + o);
                 } else {
-                    sE[idx] = fin[o];
-                    sE[idx + 1] = fin[o + 1];
-                    sX[idx] = fin[nxp + o];
-                    sX[idx + 1] = fin[nxp + o + 1];
-                    sY[idx] = fin[2 * nxp + o];
-                    sY[idx + 1] = fin[2 * nxp + o + 1];
+                    er[m] = make_float2(fin[o], fin[o + 1]);
+                    xr[m] = make_float2(fin[nxp + o], fin[nxp + o + 1]);
+                    yr[m] = make_float2(fin[2 * nxp + o], fin[2 * nxp + o + 1]);
                     cb2[m] = make_float2(cbp[o], cbp[o + 1]);
                 }
+                *reinterpret_cast<float2*>(sE + idx) = er[m];
+                *reinterpret_cast<float2*>(sX + idx) = xr[m];
+                *reinterpret_cast<float2*>(sY + idx) = yr[m];
             }
             __syncthreads();
 #pragma unroll
@@ -200,15 +202,16 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                     const int q = tid + m * BNT;
                     if (q >= NP) continue;
                     const int idx = 2 * q;
-                    const float2 e = *reinterpret_cast<const float2*>(sE + idx);
+                    const float2 e = er[m];
                     const float2 eu = *reinterpret_cast<const float2*>(sE + idx - RY);
                     const float em = sE[idx - 1];
-                    float2 hx = *reinterpret_cast<const float2*>(sX + idx);
-                    float2 hy = *reinterpret_cast<const float2*>(sY + idx);
+                    float2 hx = xr[m], hy = yr[m];
                     hx.x = h_minus(hx.x, diff(e.x, em, idy), da, db);
                     hx.y = h_minus(hx.y, diff(e.y, e.x, idy), da, db);
                     hy.x = h_plus(hy.x, diff(e.x, eu.x, idx_), da, db);
                     hy.y = h_plus(hy.y, diff(e.y, eu.y, idx_), da, db);
+                    xr[m] = hx;
+                    yr[m] = hy;
                     *reinterpret_cast<float2*>(sX + idx) = hx;
                     *reinterpret_cast<float2*>(sY + idx) = hy;
                 }
@@ -218,13 +221,13 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                     const int q = tid + m * BNT;
                     if (q >= NP) continue;
                     const int idx = 2 * q;
-                    const float2 hx = *reinterpret_cast<const float2*>(sX + idx);
-                    const float2 hy = *reinterpret_cast<const float2*>(sY + idx);
+                    const float2 hx = xr[m], hy = yr[m];
                     const float2 hyd = *reinterpret_cast<const float2*>(sY + idx + RY);
                     const float hxn = sX[idx + 2];
-                    float2 e = *reinterpret_cast<const float2*>(sE + idx);
+                    float2 e = er[m];
                     e.x = __fmaf_rn(cb2[m].x, __fsub_rn(diff(hyd.x, hy.x, idx_), diff(hx.y, hx.x, idy)), e.x);
                     e.y = __fmaf_rn(cb2[m].y, __fsub_rn(diff(hyd.y, hy.y, idx_), diff(hxn, hx.y, idy)), e.y);
+                    er[m] = e;
                     *reinterpret_cast<float2*>(sE + idx) = e;
                 }
                 __syncthreads();
@@ -239,16 +242,17 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                 const int64_t o = (int64_t)(gx0 + r) * pitch + (gy0 + c);
                 if (K % 2 == 0) {  // c even, K and TY even: both cells of the pair are in or out
                     if (c < K || c >= K + TY) continue;
-                    *reinterpret_cast<float2*>(fout + o) = *reinterpret_cast<const float2*>(sE + idx);
-                    *reinterpret_cast<float2*>(fout + nxp + o) = *reinterpret_cast<const float2*>(sX + idx);
-                    *reinterpret_cast<float2*>(fout + 2 * nxp + o) = *reinterpret_cast<const float2*>(sY + idx);
+                    *reinterpret_cast<float2*>(fout + o) = er[m];
+                    *reinterpret_cast<float2*>(fout + nxp + o) = xr[m];
+                    *reinterpret_cast<float2*>(fout + 2 * nxp + o) = yr[m];
                 } else {
+                    const float ev[2] = {er[m].x, er[m].y}, xv[2] = {xr[m].x, xr[m].y}, yv[2] = {yr[m].x, yr[m].y};
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
                         if (c + h < K || c + h >= K + TY) continue;
-                        fout[o + h] = sE[idx + h];
-                        fout[nxp + o + h] = sX[idx + h];
-                        fout[2 * nxp + o + h] = sY[idx + h];
+                        fout[o + h] = ev[h];
+                        fout[nxp + o + h] = xv[h];
+                        fout[2 * nxp + o + h] = yv[h];
                     }
                 }
             }
