@@ -273,18 +273,18 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
             // as zero and are never stored.
             constexpr int NP = RC / 2;
             constexpr int MP = (NP + BNT - 1) / BNT;
-            float2 cb2[MP];
+            float2 cb2[MP], er[MP], xr[MP], yr[MP];  // own pairs stay in registers
             unsigned fl2[2 * MP];  // per cell: bit 0 Hx, 1 Hy, 2 Ez, 3 interior; x slab << 8, y slab << 16
 #pragma unroll
             for (int m = 0; m < MP; ++m) {
                 const int q = tid + m * BNT;
-                cb2[m] = make_float2(0.f, 0.f);
+                cb2[m] = er[m] = xr[m] = yr[m] = make_float2(0.f, 0.f);
                 fl2[2 * m] = fl2[2 * m + 1] = (255u << 8) | (255u << 16);
                 if (q >= NP) continue;
                 const int idx = 2 * q;
                 const int r = idx / RY, c0 = idx - (idx / RY) * RY;
                 const int gi = gx0 + r;
-                float cbv[2];
+                float cbv[2], ev[2], xv[2], yv[2];
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const int c = c0 + h, gj = gy0 + c;
@@ -319,8 +319,14 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                     sE[idx + h] = e;
                     sX[idx + h] = hx;
                     sY[idx + h] = hy;
+                    ev[h] = e;
+                    xv[h] = hx;
+                    yv[h] = hy;
                 }
                 cb2[m] = make_float2(cbv[0], cbv[1]);
+                er[m] = make_float2(ev[0], ev[1]);
+                xr[m] = make_float2(xv[0], xv[1]);
+                yr[m] = make_float2(yv[0], yv[1]);
             }
             __syncthreads();
 #pragma unroll 1
@@ -330,11 +336,10 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                     const int q = tid + m * BNT;
                     if (q >= NP) continue;
                     const int idx = 2 * q;
-                    const float2 e = *reinterpret_cast<const float2*>(sE + idx);
+                    const float2 e = er[m];
                     const float2 eu = *reinterpret_cast<const float2*>(sE + idx - RY);
                     const float em = sE[idx - 1];
-                    float2 hx = *reinterpret_cast<const float2*>(sX + idx);
-                    float2 hy = *reinterpret_cast<const float2*>(sY + idx);
+                    float2 hx = xr[m], hy = yr[m];
                     float cy[2] = {diff(e.x, em, idy), diff(e.y, e.x, idy)};
                     float cx[2] = {diff(e.x, eu.x, idx_), diff(e.y, eu.y, idx_)};
                     float* hxp = &hx.x;
@@ -348,6 +353,8 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                         hxp[h] = (f & 1u) ? h_minus(hxp[h], cy[h], da, db) : hxp[h];
                         hyp[h] = (f & 2u) ? h_plus(hyp[h], cx[h], da, db) : hyp[h];
                     }
+                    xr[m] = hx;
+                    yr[m] = hy;
                     *reinterpret_cast<float2*>(sX + idx) = hx;
                     *reinterpret_cast<float2*>(sY + idx) = hy;
                 }
@@ -357,11 +364,10 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                     const int q = tid + m * BNT;
                     if (q >= NP) continue;
                     const int idx = 2 * q;
-                    const float2 hx = *reinterpret_cast<const float2*>(sX + idx);
-                    const float2 hy = *reinterpret_cast<const float2*>(sY + idx);
+                    const float2 hx = xr[m], hy = yr[m];
                     const float2 hyd = *reinterpret_cast<const float2*>(sY + idx + RY);
                     const float hxn = sX[idx + 2];
-                    float2 e = *reinterpret_cast<const float2*>(sE + idx);
+                    float2 e = er[m];
                     float c1[2] = {diff(hyd.x, hy.x, idx_), diff(hyd.y, hy.y, idx_)};
                     float c2[2] = {diff(hx.y, hx.x, idy), diff(hxn, hx.y, idy)};
                     float* ep = &e.x;
@@ -374,6 +380,7 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                         if ((f & 4u) && qy != 255u) c2[h] = cpml_d(c2[h], sb[qy], sa[qy], sk[qy], qZY[idx + h]);
                         ep[h] = (f & 4u) ? __fmaf_rn(cbv[h], __fsub_rn(c1[h], c2[h]), ep[h]) : ep[h];
                     }
+                    er[m] = e;
                     *reinterpret_cast<float2*>(sE + idx) = e;
                 }
                 __syncthreads();
@@ -390,9 +397,9 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                     if (!(f & 8u)) continue;
                     const int gj = gy0 + (idx + h - (idx / RY) * RY);
                     const int64_t o = (int64_t)gi * pitch + gj;
-                    fout[o] = sE[idx + h];
-                    fout[nxp + o] = sX[idx + h];
-                    fout[2 * nxp + o] = sY[idx + h];
+                    fout[o] = h ? er[m].y : er[m].x;
+                    fout[nxp + o] = h ? xr[m].y : xr[m].x;
+                    fout[2 * nxp + o] = h ? yr[m].y : yr[m].x;
                     const unsigned qx = (f >> 8) & 255u, qy = (f >> 16) & 255u;
                     if (qx != 255u) {
                         P.psi_out[pyx + (int64_t)qx * pitch + gj] = qYX[idx + h];
