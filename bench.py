@@ -178,6 +178,21 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_throughput(ms_local: float, units_per_rank: float, device=None):
+    """(max over ranks of the timed milliseconds, whole-job units per second).
+    The job ends when its slowest replica does, and every rank processed
+    ``units_per_rank``; a single process reports its own time."""
+    import torch
+
+    ws = dist_env()[0]
+    ms = float(ms_local)
+    if ws > 1 and torch.distributed.is_available() and torch.distributed.is_initialized():
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, units_per_rank * ws / (ms / 1e3)
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -299,11 +314,8 @@ def main():
     launches = eng.launch_count() - n0
     clk = clocks.stop()
     status |= eng.check_status()
-    if ws > 1:
-        t = torch.tensor([ms_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
-    value = cells * tsteps * args.steps * ws / (ms_total / 1e3) / 1e9
+    ms_total, units_per_s = replica_throughput(ms_total, cells * tsteps * args.steps, dev)
+    value = units_per_s / 1e9
 
     # roofline of the dominant kernel (fused H+E stencil, one launch = one time step)
     bpc = b_alg(DIMS)
