@@ -12,6 +12,12 @@
 // neighbouring CTA may still be reading this CTA's halo of E^n while this CTA
 // writes E^{n+1}.  The CPML psi arrays ping-pong for the same reason: halo H
 // points are computed redundantly but their psi is written only by the owner.
+//
+// Work items (tile, x-chunk) are classified by the CPML slab axes they touch;
+// each class has a kernel body compiled for exactly those axes (no CPML code for
+// the interior).  In float32 without per-cell H / Ca coefficients all classes
+// run in one launch (fused3_multi, the class stored in the item) from a single
+// longest-first queue; otherwise a plain and a general launch run on two streams.
 #include <cuda.h>
 
 #include <algorithm>
