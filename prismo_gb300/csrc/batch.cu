@@ -274,14 +274,42 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
             constexpr int NP = RC / 2;
             constexpr int MP = (NP + BNT - 1) / BNT;
             float2 cb2[MP], er[MP], xr[MP], yr[MP];  // own pairs stay in registers
-            unsigned fl2[2 * MP];  // per cell: bit 0 Hx, 1 Hy, 2 Ez, 3 interior; x slab << 8, y slab << 16
+            unsigned fl2[2 * MP];
+            // Pair order: the pairs of the y-slab columns first (row by row), then the
+            // others, so that the psi code of a y-edge tile runs in the warps that hold
+            // slab pairs only, not in every warp of the tile.  [a0, b0) and [a1, b1):
+            // the region's slab pair columns (low and high y slab, possibly empty).
+            constexpr int NPC = RY / 2;  // pairs per row
+            int pidx[MP];
+            {
+                const int a0 = max(0, -gy0) / 2, b0 = max(a0, min(RY, t - gy0) / 2 + (min(RY, t - gy0) & 1));
+                const int lo1 = max(max(0, ny - t - gy0), 2 * b0), hi1 = min(RY, ny - gy0);
+                const int a1 = lo1 / 2, b1 = max(a1, hi1 / 2 + (hi1 & 1));
+                const int ns = (b0 - a0) + (b1 - a1), nn = NPC - ns;
+#pragma unroll
+                for (int m = 0; m < MP; ++m) {
+                    const int q = tid + m * BNT;
+                    int r = 0, c2 = 0;
+                    if (q < RX * ns) {
+                        r = q / ns;
+                        const int k = q - r * ns;
+                        c2 = k < b0 - a0 ? a0 + k : a1 + (k - (b0 - a0));
+                    } else if (q < NP) {
+                        const int qq = q - RX * ns;
+                        r = qq / nn;
+                        const int k = qq - r * nn;  // k-th column outside [a0, b0) and [a1, b1)
+                        c2 = k < a0 ? k : (k - a0 + b0 < a1 ? k - a0 + b0 : k - a0 - (a1 - b0) + b1);
+                    }
+                    pidx[m] = r * RY + 2 * c2;
+                }
+            }  // per cell: bit 0 Hx, 1 Hy, 2 Ez, 3 interior; x slab << 8, y slab << 16
 #pragma unroll
             for (int m = 0; m < MP; ++m) {
                 const int q = tid + m * BNT;
                 cb2[m] = er[m] = xr[m] = yr[m] = make_float2(0.f, 0.f);
                 fl2[2 * m] = fl2[2 * m + 1] = (255u << 8) | (255u << 16);
                 if (q >= NP) continue;
-                const int idx = 2 * q;
+                const int idx = pidx[m];
                 const int r = idx / RY, c0 = idx - (idx / RY) * RY;
                 const int gi = gx0 + r;
                 float cbv[2], ev[2], xv[2], yv[2];
@@ -335,7 +363,7 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                 for (int m = 0; m < MP; ++m) {
                     const int q = tid + m * BNT;
                     if (q >= NP) continue;
-                    const int idx = 2 * q;
+                    const int idx = pidx[m];
                     const float2 e = er[m];
                     const float2 eu = *reinterpret_cast<const float2*>(sE + idx - RY);
                     const float em = sE[idx - 1];
@@ -363,7 +391,7 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                 for (int m = 0; m < MP; ++m) {
                     const int q = tid + m * BNT;
                     if (q >= NP) continue;
-                    const int idx = 2 * q;
+                    const int idx = pidx[m];
                     const float2 hx = xr[m], hy = yr[m];
                     const float2 hyd = *reinterpret_cast<const float2*>(sY + idx + RY);
                     const float hxn = sX[idx + 2];
@@ -389,7 +417,7 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
             for (int m = 0; m < MP; ++m) {
                 const int q = tid + m * BNT;
                 if (q >= NP) continue;
-                const int idx = 2 * q;
+                const int idx = pidx[m];
                 const int gi = gx0 + idx / RY;
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
