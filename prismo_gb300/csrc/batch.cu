@@ -11,20 +11,24 @@
 // One pass advances every instance by K steps (temporal blocking): a CTA loads
 // its tile plus a K-cell halo of Ez, Hx, Hy into shared memory, runs K leap-frog
 // steps there (the valid region shrinks by one cell per side per step), and
-// writes the tile interior to the other field set (ping-pong).  Items fall in two
+// writes the tile interior to the other field set (ping-pong).  Every thread owns
+// y-adjacent cell pairs and keeps them in registers across the K steps; shared
+// memory carries the values neighbouring threads read.  Items fall in three
 // classes, each with its own kernel: tiles whose region lies inside the instance
 // and clear of the CPML, the source column and the port lines take a branch-free
-// path (no per-cell tests, y-adjacent cell pairs as float2, three shared arrays);
-// the others keep per-cell validity flags and Cb in registers and the four CPML
-// auxiliaries in shared memory, add the soft mode-profile line source in the E
-// phase (sources/point.py:62-73 semantics, amplitude at t_{n+1}) and sample the
-// port DFT lines into the shared DFT ring.  The time loop is captured once as a
-// CUDA graph of G steps and replayed; a device step counter drives the amplitude
+// path (no per-cell tests, three shared arrays); tiles at the instance edges or on
+// the CPML keep per-cell flags (components the stepper does not update there, slab
+// indices) and the four CPML auxiliaries in shared memory, with their y-slab pairs
+// ordered first so that only the warps holding them run the psi code; tiles with
+// source or port cells add, on top of that, the soft mode-profile line source in
+// the E phase (sources/point.py:62-73 semantics, amplitude at t_{n+1}) and sample
+// the port DFT lines into the shared DFT ring.  The time loop is captured once as
+// a CUDA graph of G steps and replayed; a device step counter drives the amplitude
 // table.
 //
 // Arithmetic per point is that of the single-simulation 2D stepper (stepper_split.cu
-// split_h2 / split_e2 Ez family), with every rounding explicit so that both
-// classes and every tile shape give the same bits.
+// split_h2 / split_e2 Ez family), with every rounding explicit so that every
+// class and every tile shape give the same bits.
 #include <algorithm>
 #include <cstring>
 #include <numeric>
@@ -89,14 +93,14 @@ template <int TX, int TY, int K>
 struct BShape {
     static_assert(TY % 2 == 0, "the fast path moves y-adjacent pairs");
     static constexpr int RX = TX + 2 * K, RY = TY + 2 * K, RC = RX * RY, M = (RC + BNT - 1) / BNT;
-    static constexpr int MP = (RC / 2 + BNT - 1) / BNT;  // cell pairs per thread (fast path)
-    // general path: two CTAs per SM (64 registers a thread) while the per-cell
-    // registers fit; fast path: three CTAs per SM (42 registers) while its pairs fit
+    static constexpr int MP = (RC / 2 + BNT - 1) / BNT;  // cell pairs per thread
+    // two CTAs per SM (64 registers a thread) while a thread's pairs, flags and psi
+    // offsets fit; the fast path three (42 registers) for at most two pairs
     static constexpr int MINB = M <= 8 ? 2 : 1;
     static constexpr int MINB_FAST = MP <= 2 ? 3 : (MP <= 8 ? 2 : 1);
-    // Ez, Hx, Hy with RY + 2 guard cells on both sides (the fast path reads
-    // neighbours of edge cells without tests), then (general path only) the four
-    // CPML auxiliaries
+    // Ez, Hx, Hy with RY + 2 guard cells on both sides (edge cells read their
+    // neighbours without tests), then (edge and source/port items) the four CPML
+    // auxiliaries
     static constexpr int GUARD = RY + 2;  // even: the float2 accesses stay 8-byte aligned
     static constexpr int FS = RC + 2 * GUARD;
     static constexpr size_t SMEM = sizeof(float) * (3 * FS + 4 * RC);
@@ -104,8 +108,8 @@ struct BShape {
 };
 
 // The update formulas with explicit rounding (no contraction choices left to the
-// compiler), so that the fast and the general path -- and therefore every tile
-// shape -- give bit-identical fields.  Same operations as split_h2 / split_e2.
+// compiler), so that every item class -- and therefore every tile shape -- gives
+// bit-identical fields.  Same operations as split_h2 / split_e2.
 __device__ __forceinline__ float cpml_d(float d, float b, float a, float kinv, float& psi) {
     psi = __fmaf_rn(b, psi, __fmul_rn(a, d));
     return __fmaf_rn(d, kinv, psi);
@@ -119,7 +123,7 @@ __device__ __forceinline__ float h_plus(float h, float d, float da, float db) { 
 __device__ __forceinline__ float diff(float a, float b, float inv) { return __fmul_rn(__fsub_rn(a, b), inv); }
 
 // FAST: the kernel of the fast-path items (their own table and launch, with the
-// smaller shared-memory footprint and higher occupancy); otherwise the general
+// smaller shared-memory footprint and higher occupancy); otherwise the edge / CPML
 // items, SPEC: those holding source or port cells (the only ones that compile the
 // source and port-sample code; their own table and launch as well).
 template <int TX, int TY, int K, bool FAST, bool SPEC>
@@ -262,9 +266,9 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
         const int64_t pzx = pyx + 2 * (int64_t)t * pitch;  // psi Ez (x-derivative), [2t][pitch]
         const int64_t pxy = pyx + 4 * (int64_t)t * pitch;  // psi Hx (y-derivative), [nx][2t]
         const int64_t pzy = pxy + 2 * (int64_t)t * nx;     // psi Ez (y-derivative), [nx][2t]
-        if (!SPEC) {
-            // ---- CPML path: items at the instance edges or on the CPML slabs, without
-            // source or port cells.  The fast path's y-adjacent pairs and guard cells
+        {
+            // ---- paired path of the other items: at the instance edges or on the CPML
+            // slabs, and (SPEC) holding source or port cells.  The fast path's y-adjacent pairs and guard cells
             // (region-edge cells compute garbage that never reaches the shrinking valid
             // region), plus per-cell flags only where the stencil of the reference
             // stepper differs: components it does not update at the instance edges keep
@@ -302,7 +306,9 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                     }
                     pidx[m] = r * RY + 2 * c2;
                 }
-            }  // per cell: bit 0 Hx, 1 Hy, 2 Ez, 3 interior; x slab << 8, y slab << 16
+            }
+            // fl2, per cell: bit 0 Hx, 1 Hy, 2 Ez updates, 3 interior, 4 source cell,
+            // 5 port cell; x slab index << 8, y slab index << 16 (255: none)
 #pragma unroll
             for (int m = 0; m < MP; ++m) {
                 const int q = tid + m * BNT;
@@ -330,6 +336,10 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                         if (gi >= 1 && gi <= nx - 2 && gj < ny - 1) f |= 2u;
                         if (gi < nx - 1 && gj < ny - 1) f |= 4u;
                         if (r >= K && r < K + TX && c >= K && c < K + TY) f |= 8u;
+                        if (SPEC && gi == sI.src_x && (unsigned)(gj - sI.src_y0) < (unsigned)sI.src_n) f |= 16u;
+                        if (SPEC && (f & 8u))
+                            for (int q2 = 0; q2 < sI.nport; ++q2)
+                                if (gi == sI.mx[q2] && (unsigned)(gj - sI.my0[q2]) < (unsigned)sI.mn[q2]) f |= 32u;
                         if (cp) {
                             sxs = slab_idx(gi, nx, t);
                             sys = slab_idx(gj, ny, t);
@@ -359,6 +369,11 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
             __syncthreads();
 #pragma unroll 1
             for (int s = 0; s < K; ++s) {
+                double amp = 0.0;  // the source amplitude a(t_{n+1}) of this step
+                if (SPEC && P.live) {
+                    const long long n = base + P.s_off + s;
+                    if (n < P.namps) amp = P.amps[n];
+                }
 #pragma unroll
                 for (int m = 0; m < MP; ++m) {
                     const int q = tid + m * BNT;
@@ -407,6 +422,15 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                         if ((f & 4u) && qx != 255u) c1[h] = cpml_d(c1[h], sb[qx], sa[qx], sk[qx], qZX[idx + h]);
                         if ((f & 4u) && qy != 255u) c2[h] = cpml_d(c2[h], sb[qy], sa[qy], sk[qy], qZY[idx + h]);
                         ep[h] = (f & 4u) ? __fmaf_rn(cbv[h], __fsub_rn(c1[h], c2[h]), ep[h]) : ep[h];
+                        if (SPEC && (f & 4u) && (f & 48u) && P.live) {
+                            // the soft source at t_{n+1}, then the port samples (split_e2 order)
+                            const int gi = gx0 + idx / RY, gj = gy0 + (idx + h - (idx / RY) * RY);
+                            if (f & 16u) ep[h] = __fadd_rn(ep[h], static_cast<float>(P.w[sI.w_off + (gj - sI.src_y0)] * amp));
+                            if ((f & 32u) && P.ring)
+                                for (int q2 = 0; q2 < sI.nport; ++q2)
+                                    if (gi == sI.mx[q2] && (unsigned)(gj - sI.my0[q2]) < (unsigned)sI.mn[q2])
+                                        P.ring[(int64_t)(P.row0 + s) * P.npts + sI.mpt[q2] + (gj - sI.my0[q2])] = ep[h];
+                        }
                     }
                     er[m] = e;
                     *reinterpret_cast<float2*>(sE + idx) = e;
@@ -441,138 +465,6 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
             }
             continue;
         }
-        float cbr[M];
-
-        // ---- general path: per-cell validity, CPML, source and port samples ----
-        unsigned fl[M];
-#pragma unroll
-        for (int m = 0; m < M; ++m) {
-            const int idx = tid + m * BNT;
-            fl[m] = 0;
-            cbr[m] = 0.f;
-            if (idx >= RC) continue;
-            const int r = idx / RY, c = idx - (idx / RY) * RY;
-            const int gi = gx0 + r, gj = gy0 + c;
-            const bool in = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
-            float e = 0.f, hx = 0.f, hy = 0.f;
-            unsigned f = 0;
-            unsigned sxs = 255, sys = 255;
-            if (in) {
-                const int64_t o = (int64_t)gi * pitch + gj;
-                e = fin[o];
-                hx = fin[nxp + o];
-                hy = fin[2 * nxp + o];
-                cbr[m] = cbp[o];
-                f |= F_IN;
-                if (c >= 1 && gi < nx - 1 && gj >= 1 && gj <= ny - 2) f |= F_HX;
-                if (r >= 1 && gi >= 1 && gi <= nx - 2 && gj < ny - 1) f |= F_HY;
-                if (r < RX - 1 && c < RY - 1 && gi < nx - 1 && gj < ny - 1) f |= F_EZ;
-                if (r >= K && r < K + TX && c >= K && c < K + TY) f |= F_INT;
-                if (SPEC && gi == sI.src_x && (unsigned)(gj - sI.src_y0) < (unsigned)sI.src_n) f |= F_SRC;
-                if (SPEC && (f & F_INT))
-                    for (int q = 0; q < sI.nport; ++q)
-                        if (gi == sI.mx[q] && (unsigned)(gj - sI.my0[q]) < (unsigned)sI.mn[q]) f |= F_PORT;
-                if (cp) {
-                    sxs = slab_idx(gi, nx, t);
-                    sys = slab_idx(gj, ny, t);
-                    if (sxs != 255) {
-                        qYX[idx] = P.psi_in[pyx + (int64_t)sxs * pitch + gj];
-                        qZX[idx] = P.psi_in[pzx + (int64_t)sxs * pitch + gj];
-                    }
-                    if (sys != 255) {
-                        qXY[idx] = P.psi_in[pxy + (int64_t)gi * (2 * t) + sys];
-                        qZY[idx] = P.psi_in[pzy + (int64_t)gi * (2 * t) + sys];
-                    }
-                }
-            }
-            fl[m] = f | (sxs << 8) | (sys << 16);
-            sE[idx] = e;
-            sX[idx] = hx;
-            sY[idx] = hy;
-        }
-        __syncthreads();
-
-        // the step loop stays rolled: K copies of this body (M cells each, with the
-        // CPML, source and port code) overflow the instruction cache
-#pragma unroll 1
-        for (int s = 0; s < K; ++s) {
-            // H^{n+1/2} from Ez^n
-#pragma unroll
-            for (int m = 0; m < M; ++m) {
-                const int idx = tid + m * BNT;
-                const unsigned f = fl[m];
-                if (f & F_HX) {
-                    float cy = diff(sE[idx], sE[idx - 1], idy);
-                    const unsigned q = (f >> 16) & 255u;
-                    if (cp && q != 255u) cy = cpml_d(cy, sb[q], sa[q], sk[q], qXY[idx]);
-                    sX[idx] = h_minus(sX[idx], cy, da, db);
-                }
-                if (f & F_HY) {
-                    float cx = diff(sE[idx], sE[idx - RY], idx_);
-                    const unsigned q = (f >> 8) & 255u;
-                    if (cp && q != 255u) cx = cpml_d(cx, sb[q], sa[q], sk[q], qYX[idx]);
-                    sY[idx] = h_plus(sY[idx], cx, da, db);
-                }
-            }
-            __syncthreads();
-            // Ez^{n+1} from H^{n+1/2}, then the source at t_{n+1} and the port samples
-            double amp = 0.0;
-            if (SPEC && P.live) {
-                const long long n = base + P.s_off + s;
-                if (n < P.namps) amp = P.amps[n];
-            }
-#pragma unroll
-            for (int m = 0; m < M; ++m) {
-                const int idx = tid + m * BNT;
-                const unsigned f = fl[m];
-                if (f & F_EZ) {
-                    float c1 = diff(sY[idx + RY], sY[idx], idx_);
-                    float c2 = diff(sX[idx + 1], sX[idx], idy);
-                    if (cp) {
-                        const unsigned qx = (f >> 8) & 255u, qy = (f >> 16) & 255u;
-                        if (qx != 255u) c1 = cpml_d(c1, sb[qx], sa[qx], sk[qx], qZX[idx]);
-                        if (qy != 255u) c2 = cpml_d(c2, sb[qy], sa[qy], sk[qy], qZY[idx]);
-                    }
-                    float e = __fmaf_rn(cbr[m], __fsub_rn(c1, c2), sE[idx]);
-                    if (SPEC && P.live && (f & F_SRC)) {
-                        const int gj = gy0 + (idx - (idx / RY) * RY);
-                        e = __fadd_rn(e, static_cast<float>(P.w[sI.w_off + (gj - sI.src_y0)] * amp));
-                    }
-                    sE[idx] = e;
-                    if (SPEC && P.live && P.ring && (f & F_PORT)) {
-                        const int gi = gx0 + idx / RY, gj = gy0 + (idx - (idx / RY) * RY);
-                        for (int q = 0; q < sI.nport; ++q)
-                            if (gi == sI.mx[q] && (unsigned)(gj - sI.my0[q]) < (unsigned)sI.mn[q])
-                                P.ring[(int64_t)(P.row0 + s) * P.npts + sI.mpt[q] + (gj - sI.my0[q])] = e;
-                    }
-                }
-            }
-            __syncthreads();
-        }
-
-        // tile interior -> the other set
-#pragma unroll
-        for (int m = 0; m < M; ++m) {
-            const int idx = tid + m * BNT;
-            const unsigned f = fl[m];
-            if (!(f & F_INT)) continue;
-            const int gi = gx0 + idx / RY, gj = gy0 + (idx - (idx / RY) * RY);
-            const int64_t o = (int64_t)gi * pitch + gj;
-            fout[o] = sE[idx];
-            fout[nxp + o] = sX[idx];
-            fout[2 * nxp + o] = sY[idx];
-            if (cp) {
-                const unsigned qx = (f >> 8) & 255u, qy = (f >> 16) & 255u;
-                if (qx != 255u) {
-                    P.psi_out[pyx + (int64_t)qx * pitch + gj] = qYX[idx];
-                    P.psi_out[pzx + (int64_t)qx * pitch + gj] = qZX[idx];
-                }
-                if (qy != 255u) {
-                    P.psi_out[pxy + (int64_t)gi * (2 * t) + qy] = qXY[idx];
-                    P.psi_out[pzy + (int64_t)gi * (2 * t) + qy] = qZY[idx];
-                }
-            }
-        }
     }
 }
 
@@ -582,7 +474,7 @@ __global__ void batch_advance(long long* step, int n) {
 
 struct Variant {
     int tx, ty, k, k1;  // tile, steps per pass, index of the K=1 sibling
-    const void* fn[3];  // [0]: fast-path items, [1]: general items, [2]: source / port items
+    const void* fn[3];  // [0]: fast-path items, [1]: edge / CPML items, [2]: source / port items
     size_t smem[3];
 };
 
@@ -635,9 +527,9 @@ struct pc_batch {
     int variant = 1;
     int graph_steps = 80;
     int item_variant = -1;
-    int4* d_items = nullptr;  // fast-path items, then general items, then source / port items
+    int4* d_items = nullptr;  // fast-path items, then edge / CPML items, then source / port items
     int nitems = 0;
-    int nfast = 0, ngen = 0;  // fast items, then general ones, then source / port ones
+    int nfast = 0, ngen = 0;  // fast items, then edge / CPML ones, then source / port ones
     int items_cap = 0;
     int grid[kNumVariants][3] = {};
     cudaStream_t cap_stream = nullptr;
@@ -674,7 +566,8 @@ int build_items(pc_batch* b, int v) {
             for (int y0 = 0; y0 < ny; y0 += V.ty) {
                 const int ax0 = x0 - K, ax1 = x0 + V.tx + K, ay0 = y0 - K, ay1 = y0 + V.ty + K;
                 // bit 0: the region (with its halo) reaches the CPML or the instance edge
-                // bit 1: it holds source or port cells (both take the general path)
+                // bit 1: it holds source or port cells (own class: the source and
+                // port-sample code)
                 const bool cp = ax0 < t || ax1 > nx - t || ay0 < t || ay1 > ny - t || ax0 < 0 || ay0 < 0 ||
                                 ax1 > nx || ay1 > ny;
                 const pc_batch_instance& d = b->desc[n];
@@ -691,7 +584,7 @@ int build_items(pc_batch* b, int v) {
     if (b->d_items) drop_graphs(b);  // captured graphs hold the previous table
     std::vector<int> ord(items.size());
     std::iota(ord.begin(), ord.end(), 0);
-    // fast-path items first, then the general ones without and then those with
+    // fast-path items first, then the edge / CPML ones without and then those with
     // source or port cells; each class longest first
     auto cls = [&](int a) { return (items[a].w & 2) ? 2 : ((items[a].w & 1) ? 1 : 0); };
     std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) {
@@ -765,8 +658,9 @@ BPass make_pass(pc_batch* b, int s_off, int row0, bool live) {
     return P;
 }
 
-// One pass = the fast-path items' kernel, then the general items' kernel; returns
-// the number of kernels launched (or a negative error).
+// One pass = the fast-path items' kernel, then the edge / CPML items' kernel, then
+// the source / port items' kernel; returns the number of kernels launched (or a
+// negative error).
 int launch_pass(pc_batch* b, int v, const BPass& P0, cudaStream_t s) {
     int launched = 0;
     for (int path = 0; path < 3; ++path) {
