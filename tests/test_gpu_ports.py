@@ -7,7 +7,7 @@ plane and interpolated profiles are pinned to the reference in test_host_api.py.
 import numpy as np
 import pytest
 
-from test_host_api import _port_modes
+from helpers import port_modes
 
 pytestmark = pytest.mark.gpu
 
@@ -42,7 +42,7 @@ def test_mode_port_inject_and_extract(pg, dtype):
 
     rng = np.random.default_rng(12)
     grid = YeeGrid(GridSpec(size=(1.2e-6, 1.0e-6, 0.8e-6), resolution=20e6))
-    modes = _port_modes(rng)
+    modes = port_modes(rng)
     for direction, center, size in (("+x", (0.5e-6, 0.5e-6, 0.4e-6), (0.0, 0.6e-6, 0.5e-6)),
                                     ("-y", (0.6e-6, 0.45e-6, 0.4e-6), (0.7e-6, 0.0, 0.5e-6)),
                                     ("+z", (0.6e-6, 0.5e-6, 0.3e-6), (0.7e-6, 0.6e-6, 0.0))):

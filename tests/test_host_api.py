@@ -248,9 +248,9 @@ def test_tensor_material_matches_reference_inverses():
     """prismo_gb300.tensor containers against the reference's TensorMaterial
     (materials/tensor.py:110-312): full matrices, diagonal test, inverses."""
     from prismo_gb300.tensor import TensorComponents, TensorMaterial
-    from test_plugin import SOURCE_TREES, _import_reference
+    from helpers import SOURCE_TREES, import_reference
 
-    _import_reference(SOURCE_TREES)
+    import_reference(SOURCE_TREES)
     from prismo.materials import tensor as RT
 
     rng = np.random.default_rng(2)
@@ -266,38 +266,23 @@ def test_tensor_material_matches_reference_inverses():
         np.testing.assert_allclose(ours.get_inverse_mu(), ref.get_inverse_mu(), rtol=1e-14)
 
 
-def _port_modes(rng, n=2):
-    """Synthetic waveguide modes on their own (x, y) grid (modes/solver.py:17-53 fields)."""
-    from types import SimpleNamespace
-
-    u = np.linspace(0.1e-6, 0.9e-6, 23)
-    v = np.linspace(0.05e-6, 0.7e-6, 17)
-    U, V = np.meshgrid(u, v, indexing="ij")
-    out = []
-    for k in range(n):
-        g = np.exp(-((U - 0.5e-6) ** 2 + (V - 0.35e-6) ** 2) / (0.15e-6) ** 2)
-        f = {c: g * (rng.uniform(0.5, 1.5) + 1j * rng.uniform(-0.5, 0.5)) for c in ("Ex", "Ey", "Ez")}
-        f.update({c: g * (rng.uniform(-0.01, 0.01) + 1j * rng.uniform(-0.01, 0.01)) for c in ("Hx", "Hy", "Hz")})
-        out.append(SimpleNamespace(mode_number=k, neff=2.4 - 0.1 * k, frequency=193e12 + 5e12 * k,
-                                   wavelength=299792458.0 / (193e12 + 5e12 * k), x=u, y=v, power=1.0, **f))
-    return out
-
-
 def test_mode_port_region_and_interpolation_match_reference():
     """ModePort's plane bounds and interpolated profiles against the reference's
     own ModePort (boundaries/mode_port.py:112-259) on the same grid and modes."""
     from prismo_gb300.grid import GridSpec, YeeGrid
     from prismo_gb300.ports import ModePort, ModePortConfig
-    from test_plugin import SOURCE_TREES, _import_reference
+    from helpers import SOURCE_TREES, import_reference
 
-    _import_reference(SOURCE_TREES)
+    import_reference(SOURCE_TREES)
     from prismo.boundaries import mode_port as RP
     from prismo.core.grid import GridSpec as RGridSpec
     from prismo.core.grid import YeeGrid as RYeeGrid
     from prismo.modes.solver import WaveguideMode
 
     rng = np.random.default_rng(4)
-    modes = _port_modes(rng)
+    from helpers import port_modes
+
+    modes = port_modes(rng)
     rmodes = [WaveguideMode(**vars(m)) for m in modes]
     spec = dict(size=(1.2e-6, 1.0e-6, 0.8e-6), resolution=20e6)
     for direction, center, size in (("+x", (0.5e-6, 0.5e-6, 0.4e-6), (0.0, 0.6e-6, 0.5e-6)),

@@ -9,34 +9,8 @@ import sys
 import numpy as np
 import pytest
 
-# the reference package: an installed copy under baseline/_ref (travels with the
-# repository to GPU machines), or the source tree of a local checkout (CPU tests)
-INSTALLED = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "baseline", "_ref")
-SOURCE_TREES = [os.environ.get("PRISMO_REFERENCE_SRC", ""), "/root/reference/src"]
-
-
-def _import_reference(candidates):
-    import builtins
-    import types
-
-    for path in candidates:
-        if path and os.path.isdir(os.path.join(path, "prismo")):
-            builtins.MTLBuffer = object
-            pl = types.ModuleType("polars")
-            pl.DataFrame = object
-            sys.modules.setdefault("polars", pl)
-            try:  # a reference dependency absent on some machines; only the sweep uses it
-                import tqdm  # noqa: F401
-            except ImportError:
-                tq = types.ModuleType("tqdm")
-                tq.tqdm = lambda it=None, *a, **k: it
-                sys.modules["tqdm"] = tq
-            if path not in sys.path:
-                sys.path.insert(0, path)
-            import prismo
-
-            return prismo
-    pytest.skip("reference package not available")
+from helpers import INSTALLED, SOURCE_TREES  # noqa: F401
+from helpers import import_reference as _import_reference
 
 
 def _registered(candidates):
