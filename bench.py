@@ -244,9 +244,10 @@ def main():
                     help="x-chunk lengths 'CX[,EDGE]' of the fused schedule instead of autotuning (profiling runs)")
     ap.add_argument("--dims", type=int, default=None,
                     help="cube edge for a reduced profiling case (default: the 256^3 workload)")
-    ap.add_argument("--workload", default="3d", choices=["3d", "2d", "dispersive", "sweep", "surrogate"],
+    ap.add_argument("--workload", default="3d", choices=["3d", "2d", "dispersive", "sweep", "surrogate", "mlp"],
                     help="3d: the headline 256^3 CPML workload; dispersive: 384x384x192 Drude-Lorentz + TFSF + "
-                         "64-frequency DFT planes; sweep: 64 batched couplers; surrogate: train + held-out pipeline")
+                         "64-frequency DFT planes; sweep: 64 batched couplers; surrogate: train + held-out pipeline; "
+                         "mlp: the surrogate's forward products alone (tcgen05 and mma.sync)")
     ap.add_argument("--designs", type=int, default=64, help="designs per batched sweep")
     args = ap.parse_args()
     if args.workload != "3d":
@@ -455,6 +456,8 @@ def run_other(args):
         return run_2d(args)
     if args.workload == "sweep":
         return run_sweep(args, cpu, peak, peak_kind)
+    if args.workload == "mlp":
+        return run_mlp(args)
     return run_surrogate(args, cpu)
 
 
@@ -705,6 +708,51 @@ def run_surrogate(args, cpu):
           e2e={"value": res.designs_per_s, "unit": "designs/s", "h2d_bytes_per_step": len(test) * 12,
                "d2h_bytes_per_step": len(test) * 512 * 4, "api": "prismo_gb300.surrogate.run_pipeline"},
           cpu_baseline=cpu, gpu_launches=E.launches)
+
+
+def run_mlp(args):
+    """The surrogate ensemble's forward pass alone: 4 members x 8192 query rows
+    through 31-256-256-256-512 (bf16 hi/lo activations, float32 accumulation), on
+    the tcgen05 path and on the mma.sync path; one bench step = one forward."""
+    import torch
+
+    from prismo_gb300 import surrogate as Su
+
+    E = Su.Ensemble()
+    B = 8192
+    rng = np.random.default_rng(0)
+    E.set_params(rng.normal(0.0, 0.05, E.params().shape))  # every layer non-zero
+    x = torch.tensor(rng.standard_normal((E.members, B, E.dims[0])).astype(np.float32), device="cuda")
+    dims = E.dims
+    flops = E.members * B * 2 * (32 * dims[1] + dims[1] * dims[2] + dims[2] * dims[3] + dims[3] * dims[4])
+
+    def timed(tc):
+        E.set_tensor_path(tc)
+        for _ in range(max(args.warmup, 3)):
+            E.forward_raw(x)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = E.launches
+        ev0.record()  # the ensemble launches on torch's current stream
+        for _ in range(args.steps):
+            E.forward_raw(x)
+        ev1.record()
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / args.steps, (E.launches - n0) // max(args.steps, 1)
+
+    ms_mma, _ = timed(False)
+    ms_tc, launches = timed(True)
+    y_tc = E.forward_raw(x)
+    E.set_tensor_path(False)
+    y_mma = E.forward_raw(x)
+    rel = float((y_tc - y_mma).norm() / y_mma.norm().clamp_min(1e-30))
+    status = E.status()
+    E.close()
+    _line(metric="TFLOP/s", value=flops / (ms_tc * 1e-3) / 1e12, unit="TFLOP/s", steps=args.steps,
+          warmup=args.warmup, ms_per_step=ms_tc, dtype="bf16 (f32 accumulate)",
+          config={"workload": "surrogate forward: 4 members x 8192 rows, 31-256-256-256-512 SiLU, bf16 hi/lo "
+                              "activations", "status": status, "tcgen05_vs_mma_sync_rel": rel},
+          mma_sync_ms_per_step=ms_mma, gpu_launches=launches)
 
 
 if __name__ == "__main__":
