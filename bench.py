@@ -127,7 +127,7 @@ class ClockSampler:
 
 def make_engine(eps, precision="fp32", dims=DIMS):
     from prismo_gb300.engine import FDTDEngine
-    from prismo_gb300.grid import GridSpec, YeeGrid
+    from prismo_gb300.grid import YeeGrid
     from prismo_gb300.pml import PMLParams
     from prismo_gb300.sources import GaussianPulse
 

@@ -11,7 +11,7 @@ from __future__ import annotations
 import math
 import warnings
 from abc import ABC, abstractmethod
-from typing import Any, Optional
+from typing import Optional
 
 import numpy as np
 

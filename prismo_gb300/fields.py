@@ -8,8 +8,6 @@ fused stepper's ping-pong.
 
 from __future__ import annotations
 
-from typing import Optional
-
 import numpy as np
 
 from .backend import CudaBackend, DeviceArray, resolve

@@ -81,7 +81,6 @@ def register(prismo_module=None) -> None:
         return getattr(bm._CURRENT_BACKEND, "name", None) == "cuda"
 
     from . import fields as nf
-    from . import simulation as nsim
     from . import solver as ns
 
     def reroute(ref_cls, native_cls, adapt=None):

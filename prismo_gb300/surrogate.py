@@ -24,7 +24,7 @@ import ctypes as C
 import math
 import time
 from dataclasses import dataclass
-from typing import List, Optional, Sequence
+from typing import Sequence
 
 import numpy as np
 

@@ -2,7 +2,6 @@
 float64 autograd, and of the surrogate's output representation."""
 
 import numpy as np
-import pytest
 
 from oracle import mlp64
 

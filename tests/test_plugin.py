@@ -4,7 +4,6 @@ cuda backend when a GPU is present).  The reference is imported from its source
 tree (the harness shim of tests/golden/make_golden.py); skipped when absent."""
 
 import os
-import sys
 
 import numpy as np
 import pytest
