@@ -519,11 +519,41 @@ def run_2d(args):
     t0 = time.perf_counter()
     o.run(50)
     cpu_s = (time.perf_counter() - t0) / 50
+    # The same simulation as a one-instance batch (csrc/batch.cu: K steps per launch
+    # in shared memory): a secondary figure beside the drop-in engine's.  Fields
+    # after one run from zero are compared with the engine's; the timed run
+    # continues the same instance (the work does not depend on the field values).
+    one()
+    eng.synchronize()
+    from prismo_gb300 import sweep as S
+
+    core = np.asarray(src[1]).ravel()
+    line = np.asarray(mon[1]).ravel()
+    inst = S.Instance(eps=np.ascontiguousarray(eps[:, :, 0] if eps.ndim == 3 else eps), src=S.Port(int(np.ravel(src[0])[0]), int(core[0]), int(core.size), np.ones(core.size)),
+                      ports=[S.Port(int(np.ravel(mon[0])[0]), int(line[0]), int(line.size), np.ones(line.size))])
+    B = S.BatchedFDTD2D([inst], freqs, dx=cfg["dx"], dt=dt, cpml=cfg["cpml"])
+    B.set_amplitudes(amps[:, 0])
+    B.step(n)
+    ez_b = B.fields(0)[0].float()
+    ez_e = eng.component("Ez").float()
+    r, c = min(ez_b.shape[0], ez_e.shape[0]), min(ez_b.shape[1], ez_e.shape[1])
+    batch_rel = float((ez_b[:r, :c] - ez_e[:r, :c]).norm() / ez_e[:r, :c].norm().clamp_min(1e-30))
+    bev0, bev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    bev0.record(B.stream)
+    B.step(n)
+    bev1.record(B.stream)
+    torch.cuda.synchronize()
+    batch_ms = bev0.elapsed_time(bev1)
+    batch_tile = S.BatchedFDTD2D.variants()[B.tuning()[0]]
+    B.close()
     _line(metric="Gcell-updates/s", value=cells * n / (ms / 1e3) / 1e9, unit="Gcell/s", steps=args.steps,
           warmup=args.warmup, ms_per_step=ms, dtype="f32",
           config={"workload": "2d_te_waveguide_500x250: 20-cell CPML, slab waveguide, soft Ez line source, "
                               "11-frequency DFT line, 3000 steps (L2-resident grid)",
                   "time_steps_per_s": n / (ms / 1e3), "l2": "grid fits L2 (launch/latency bound)"},
+          same_simulation_on_batch_engine={"gcell_per_s": cells * n / (batch_ms / 1e3) / 1e9,
+                                           "time_steps_per_s": n / (batch_ms / 1e3), "tile_steps": batch_tile,
+                                           "ez_rel_l2_vs_engine": batch_rel},
           cpu_baseline={"value": cells / cpu_s / 1e9, "unit": "Gcell/s", "cores": 1, "kind": "port",
                         "sample": f"50 of 3000 steps, float64 oracle, {cpu_s * 1e3:.1f} ms/step"},
           gpu_launches=eng.launch_count() - n0, clocks=clk)
