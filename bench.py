@@ -57,6 +57,17 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def _profile_value(name, dims, key):
+    """A figure from a committed ncu summary (profiles/<name>) for the grid it covers."""
+    p = os.path.join(ROOT, "profiles", name)
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        if tuple(d.get("dims", ())) == tuple(dims):
+            return d.get(key)
+    return None
+
+
 def traffic_from_profile(dims):
     """DRAM bytes per launch of the fused kernel from the committed ncu summary
     (None for a grid the summary does not cover)."""
@@ -608,7 +619,9 @@ def run_dispersive(args, peak, peak_kind):
                               "plane wave (-z, Ex), two 64-frequency Ex DFT planes, 12-cell CPML",
                   "time_steps_per_step": per, "status": status, "l2": "inputs larger than L2"},
           roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                    "peak_kind": peak_kind, "traffic": None, "bytes_per_cell_update": bpc,
+                    "peak_kind": peak_kind, "traffic": _profile_value("dispersive_384.json", dims,
+                                                                        "dram_bytes_per_step"),
+                    "bytes_per_cell_update": bpc,
                     "kernel": "split H + E(ADE) + TFSF stencil per step", "avg_launch_us": avg * 1e6},
           gpu_launches=eng.launch_count() - n0, clocks=clk)
     eng.close()
