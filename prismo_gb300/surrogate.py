@@ -283,8 +283,9 @@ class Ensemble:
             return np.ascontiguousarray(np.broadcast_to(x[None], (self.members,) + x.shape), dtype=np.float32)
         return embed(x, self.B)
 
-    def predict(self, designs: Sequence[SW.CouplerDesign], nfreq: int = SW.NFREQ):
-        """Ensemble mean S [n][4][nf], spread [n] and per-member S [members][n][4][nf]."""
+    def predict(self, designs: Sequence[SW.CouplerDesign], nfreq: int = SW.NFREQ, members: bool = False):
+        """Ensemble mean S [n][4][nf], spread [n] and (``members``) per-member S
+        [members][n][4][nf] (None otherwise)."""
         torch = self.torch
         X = self._features(inputs(designs))
         n = X.shape[1]
@@ -298,7 +299,7 @@ class Ensemble:
         mean = y.mean(axis=0)
         ph = phase_factors(designs, nfreq)
         S = from_real(mean, nfreq) / ph
-        S_m = np.stack([from_real(y[m], nfreq) / ph for m in range(self.members)])
+        S_m = np.stack([from_real(y[m], nfreq) / ph for m in range(self.members)]) if members else None
         return S, spread, S_m
 
     def close(self):
