@@ -296,3 +296,43 @@ def test_mode_port_region_and_interpolation_match_reference():
         for a, b in zip(ours._interpolated_modes, ref._interpolated_modes):
             for c in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz"):
                 np.testing.assert_array_equal(getattr(a, c), getattr(b, c))
+
+
+def test_monitor_port_and_tensor_error_paths():
+    """Errors the reference raises (monitors/flux.py:247-248, mode_monitor.py:63-64,
+    246-256) and the device classes' own input checks, without a GPU."""
+    from types import SimpleNamespace
+
+    from prismo_gb300 import FluxMonitor, ModeExpansionMonitor
+    from prismo_gb300.grid import GridSpec, YeeGrid
+    from prismo_gb300.ports import ModePort, ModePortConfig
+
+    grid = YeeGrid(GridSpec(size=(1e-6, 0.8e-6, 0.0), resolution=20e6))
+    m = FluxMonitor(center=(0.5e-6, 0.4e-6, 0), size=(0, 0.4e-6, 0), direction="x")
+    m.initialize(grid)
+    with pytest.raises(RuntimeError):
+        m.get_frequency_domain_power()
+    assert m.get_transmission() == 0.0  # no steps yet: the reference returns 0.0
+    with pytest.raises(ValueError):
+        ModeExpansionMonitor(center=(0, 0, 0), size=(0, 1e-6, 0), modes=[], direction="q")
+    mm = ModeExpansionMonitor(center=(0.5e-6, 0.4e-6, 0), size=(0, 0.4e-6, 0), modes=[])
+    mm.initialize(grid)
+    with pytest.raises(ValueError):
+        mm.get_mode_coefficient(0, domain="space")
+    with pytest.raises(RuntimeError):
+        mm.get_mode_transmission(0)
+    port = ModePort(ModePortConfig((0.5e-6, 0.4e-6, 0), (0, 0.4e-6, 0), "+x", []))
+    with pytest.raises(ValueError):
+        port.initialize(grid)  # mode ports index [x, y, z]: 3D grids only
+    assert port.sign == 1 and port.axis == "x"
+    assert ModePort(ModePortConfig((0, 0, 0), (0, 0, 0), "-z", [])).sign == -1
+
+
+def test_anisotropic_updater_rejects_host_arrays():
+    torch = pytest.importorskip("torch")
+    from prismo_gb300.tensor import AnisotropicUpdater, TensorComponents, TensorMaterial
+
+    up = AnisotropicUpdater(TensorMaterial(TensorComponents(xx=2.0, yy=2.0, zz=2.0)), 1e-17)
+    x = [torch.zeros(4, 4, dtype=torch.float64) for _ in range(3)]
+    with pytest.raises(TypeError):
+        up.update_e_from_curl_h(x, x)
