@@ -95,3 +95,32 @@ def test_batch_create_rejects_bad_instances_without_gpu(lib):
     out = (ctypes.c_int32 * 3)()
     assert lib.pc_batch_variant_info(0, out) == 0 and out[2] == 1
     assert lib.pc_batch_variant_info(99, out) == _lib.PC_ERR_INVALID
+
+
+def test_monitor_port_tensor_entry_points_reject_bad_args_without_gpu(lib):
+    """The plane-monitor, mode-port and anisotropic entry points validate their
+    arguments before any CUDA call."""
+    from prismo_gb300 import _lib
+
+    INV = _lib.PC_ERR_INVALID
+    comps = (ctypes.c_int32 * 4)(1, 5, 2, 4)
+    offs = (ctypes.c_int64 * 4)(0, 0, 0, 0)
+    w = (ctypes.c_double * 8)()
+    n = ctypes.c_int64(0)
+    assert lib.pc_add_flux(None, comps, offs, 1, 1.0, None, 16) == INV
+    assert lib.pc_flux_count(None, 0, ctypes.byref(n), None) == INV
+    assert lib.pc_flux_spectrum(None, comps, 1.0, None, None) == INV
+    assert lib.pc_add_mode_monitor(None, comps, offs, 1, 1, w, None, 16) == INV
+    assert lib.pc_mode_count(None, 0, ctypes.byref(n), None) == INV
+    assert lib.pc_mode_spectrum(None, 0, w, 1, 0.0, 1e-17, None, None) == INV
+    P3 = ctypes.c_void_p * 3
+    nul = P3(None, None, None)
+    assert lib.pc_aniso_update(2, 1, 1, nul, nul, nul, 4, None, w, 1.0, None) == INV  # precision
+    assert lib.pc_aniso_update(4, 1, 0, nul, nul, nul, 4, None, w, 1.0, None) == INV  # sign
+    assert lib.pc_aniso_update(4, 1, 1, nul, nul, nul, 4, None, None, 1.0, None) == INV  # no coefficients
+    assert lib.pc_aniso_update(4, 1, 1, nul, nul, nul, 4, None, w, 1.0, None) == INV  # null arrays
+    assert lib.pc_scatter_add(4, None, None, None, 4, 1.0, None) == INV
+    assert lib.pc_scatter_add(3, None, None, None, 0, 1.0, None) == INV
+    P4 = ctypes.c_void_p * 4
+    assert lib.pc_plane_overlap(4, P4(None, None, None, None), None, 1, 1, None, None, None) == INV
+    assert lib.pc_plane_overlap(8, None, None, 0, 1, None, None, None) == INV
