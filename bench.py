@@ -1,8 +1,9 @@
 """Benchmark: 3D FP32 CPML FDTD, 256^3 cells, 2000 time steps (one "step" of this
 benchmark = one whole 2000-time-step simulation from zero fields).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-    python bench.py --workload dispersive|sweep|surrogate   (the other configurations)
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--chunk CX[,EDGE]]
+    python bench.py --workload 2d|dispersive|sweep|surrogate   (the other configurations)
+    python bench.py --workload mlp                             (the surrogate's forward products)
 
 Workload (the reference's 3D plain-FDTD configuration): 256^3 total cells at
 dx = 20 nm with a 12-cell CPML on all six faces, Courant 0.5, 32 seeded
