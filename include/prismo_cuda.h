@@ -6,11 +6,13 @@
  * selects an array provider (backends/backend_manager.py:139-186) and
  * `MaxwellUpdater.step` (core/solver.py:535-552) advances the Yee fields with
  * array slicing.  A "cuda" backend binds these entry points through ctypes from
- * Python; every pointer argument named `d_*` is a device
- * pointer owned by the caller, every other pointer is host memory.
+ * Python; every pointer argument named `d_*` is a device pointer owned by the
+ * caller, every other pointer is host memory.
  *
  * Conventions
- *   - Every call returns 0 (PC_OK) or a negative PC_ERR_* code.
+ *   - Every call returns 0 (PC_OK) or a negative PC_ERR_* code, except
+ *     pc_fused_steps_noalloc, which returns the index (0 or 1) of the field set
+ *     holding its result, or a negative PC_ERR_* code.
  *   - Field buffers use one padded layout for all six components:
  *       3D: element (i, j, k) at ((i*ny + j) * pitch + k)
  *       2D: element (i, j)    at (i * pitch + j)
@@ -280,7 +282,12 @@ int pc_profile_read(pc_ctx* ctx, double* total_ms, int64_t* count);
  *   - Every call shares the array and resets the status word at its start;
  *     calls that overlap on the GPU race.
  *   - status_out (host, nullable) receives the PC_STATUS_* bits; passing it
- *     synchronises the stream. */
+ *     synchronises the stream.  Without it, non-finite fields and a bounded
+ *     wait that ran out (PC_STATUS_NONFINITE, PC_STATUS_TIMEOUT) are not
+ *     reported: the next call clears the word before anyone can read it.
+ *   - The device address is cached per device index for the life of the
+ *     process; after cudaDeviceReset on a device, do not call this entry point
+ *     on that device again. */
 int pc_fused_steps_noalloc(const pc_grid_desc* desc, void* const set0[6], void* const set1[6], int32_t cur,
                            const void* const cb[3], int32_t nsteps, void* stream, uint32_t* status_out);
 
@@ -355,7 +362,15 @@ int pc_batch_autotune(pc_batch* b, int32_t passes, float* ms_per_step, void* str
 int pc_batch_step(pc_batch* b, int32_t nsteps, void* stream);
 int pc_batch_dft_flush(pc_batch* b, void* stream);
 int pc_batch_current_set(const pc_batch* b);
+/* Status words (PC_STATUS_* bits).  pc_batch_status reads the batch's word;
+ * pc_batch_instance_status reads one word per instance into flags[ninst] and
+ * clears them (synchronises the stream).  A pass that stores a NaN or Inf in
+ * an instance's Ez sets PC_STATUS_NONFINITE in that instance's word and in the
+ * batch word, so a caller can re-run just the failed designs on the
+ * per-simulation path (ParameterSweep marks a failed point and goes on,
+ * optimization/sweep.py:183-195). */
 int pc_batch_status(pc_batch* b, uint32_t* flags, void* stream);
+int pc_batch_instance_status(pc_batch* b, uint32_t* flags, void* stream);
 int64_t pc_batch_launch_count(const pc_batch* b);
 int64_t pc_batch_steps_done(const pc_batch* b);
 void pc_batch_destroy(pc_batch* b);

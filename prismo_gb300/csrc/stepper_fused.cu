@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "pc_internal.cuh"
 #include "stencil_common.cuh"
@@ -637,8 +638,9 @@ template <typename T, int TY, int TZ, int S>
 int choose_chunk(const pc_grid_desc& g, int smem) {
     auto kern = fused3<T, TY, TZ, S, 7, false, false>;
     constexpr int threads = TZ * (TY / 2 + 1);
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    int sms = 0, dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 152;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * PC_MAX_CPML * (int)sizeof(T));
@@ -842,12 +844,17 @@ __global__ void noalloc_fill_items(int4* items, int ntk, int ntj, int nchunks, i
 }  // namespace
 
 namespace {
+// Host-side cache of the scratch array's device address, one entry per device
+// index, filled on the first call on that device under a lock.  A
+// cudaDeviceReset ends the context the address belongs to; the entry is then
+// stale and the library must not be called on that device again.
+std::mutex g_noalloc_lock;
 int g_noalloc_ready[128];
 int4* g_noalloc_ptr[128];
 
 template <typename T>
-int noalloc_run(const pc_grid_desc& g, void* const set0[6], void* const set1[6], int cur, const void* const cb[3],
-                int nsteps, cudaStream_t s, int4* scratch) {
+int noalloc_run(int dev, const pc_grid_desc& g, void* const set0[6], void* const set1[6], int cur,
+                const void* const cb[3], int nsteps, cudaStream_t s, int4* scratch) {
     constexpr int TY = 16, TZ = 32, S = (sizeof(T) == 4) ? 4 : 3;
     using G = FusedGeom<T, TY, TZ>;
     auto kern = fused3<T, TY, TZ, S, 0, false, false>;
@@ -856,7 +863,7 @@ int noalloc_run(const pc_grid_desc& g, void* const set0[6], void* const set1[6],
     const int ntk = (g.nz + TZ - 1) / TZ, ntj = (g.ny + TY - 1) / TY;
     // x-chunk: about 8 work items per resident CTA, within the scratch capacity
     int sms = 0, per_sm = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TZ * (TY / 2 + 1), smem);
     const double want = 8.0 * (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
     int cx = g.nx;
@@ -924,6 +931,7 @@ extern "C" int pc_fused_steps_noalloc(const pc_grid_desc* d, void* const set0[6]
     if (d->ndim != 3 || d->mode != PC_MODE_CORRECTED || (d->precision != 4 && d->precision != 8))
         return PC_ERR_INVALID;
     if (d->nx < 3 || d->ny < 3 || d->nz < 3 || d->pitch < d->nz || d->pitch % 32 != 0) return PC_ERR_INVALID;
+    if ((int64_t)d->nx * d->ny * d->pitch > ((int64_t)1 << 40)) return PC_ERR_INVALID;
     if (!(d->dt > 0) || !(d->dx > 0) || !(d->dy > 0) || !(d->dz > 0)) return PC_ERR_INVALID;
     for (int q = 0; q < 6; ++q)
         if (!set0[q] || !set1[q]) return PC_ERR_INVALID;
@@ -932,29 +940,30 @@ extern "C" int pc_fused_steps_noalloc(const pc_grid_desc* d, void* const set0[6]
     int dev = 0;
     PC_CUDA_CHECK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 128) return PC_ERR_INVALID;
-    if (!g_noalloc_ready[dev]) {
-        // first call on this device (the device is current): resolve the device
-        // address of the scratch array; host code may not use the symbol itself
-        void* ptr = nullptr;
-        PC_CUDA_CHECK(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
-        g_noalloc_ptr[dev] = static_cast<int4*>(ptr);
-        g_noalloc_ready[dev] = 1;
+    int4* scratch = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_lock);
+        if (!g_noalloc_ready[dev]) {
+            // first call on this device (the device is current): resolve the device
+            // address of the scratch array; host code may not use the symbol itself
+            void* ptr = nullptr;
+            PC_CUDA_CHECK(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+            g_noalloc_ptr[dev] = static_cast<int4*>(ptr);
+            g_noalloc_ready[dev] = 1;
+        }
+        scratch = g_noalloc_ptr[dev];
     }
     cudaStream_t s = (cudaStream_t)stream;
-    const int rc = d->precision == 8
-                       ? noalloc_run<double>(*d, set0, set1, cur, cb, nsteps, s, g_noalloc_ptr[dev])
-                       : noalloc_run<float>(*d, set0, set1, cur, cb, nsteps, s, g_noalloc_ptr[dev]);
+    const int rc = d->precision == 8 ? noalloc_run<double>(dev, *d, set0, set1, cur, cb, nsteps, s, scratch)
+                                     : noalloc_run<float>(dev, *d, set0, set1, cur, cb, nsteps, s, scratch);
     if (rc < 0) return rc;
     if (status_out) {
-        PC_CUDA_CHECK(cudaMemcpyAsync(status_out, g_noalloc_ptr[dev] + PC_NOALLOC_MAX_ITEMS, sizeof(uint32_t),
+        PC_CUDA_CHECK(cudaMemcpyAsync(status_out, scratch + PC_NOALLOC_MAX_ITEMS, sizeof(uint32_t),
                                       cudaMemcpyDeviceToHost, s));
         PC_CUDA_CHECK(cudaStreamSynchronize(s));
     }
     return rc;
 }
-
-namespace {
-}  // namespace
 
 int launch_fused_step(pc_ctx* c, cudaStream_t s) {
     if (c->g.ndim != 3) return launch_split_step(c, s);
