@@ -20,20 +20,30 @@ def _axis_mask(n: int, centre: float, size: float) -> np.ndarray:
     return np.abs(pts - centre) <= size / 2.0
 
 
+def box_specs_3d(dims, nboxes=32, seed=0, edge=(10, 80), eps_range=(1.0, EPS_SI)):
+    """The seeded boxes of the 3D FP32 plane configuration, in draw order:
+    (centre, edges, eps) with the centre uniform in the domain and the edges
+    integer-uniform in ``edge``, both in cells; eps uniform in ``eps_range``."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(nboxes):
+        c = rng.uniform(0.0, 1.0, size=3) * np.array(dims, dtype=np.float64)
+        e = rng.integers(edge[0], edge[1] + 1, size=3)
+        v = rng.uniform(*eps_range)
+        out.append((c, e, v))
+    return out
+
+
 def boxes_3d(dims, nboxes=32, seed=0, edge=(10, 80), eps_range=(1.0, EPS_SI), background=EPS_SIO2):
     """Dielectric of seeded axis-aligned boxes (3D FP32 plane configuration).
 
-    Centres are uniform in the domain (cells), edges integer-uniform in
-    ``edge`` cells per axis, permittivities uniform in ``eps_range``; painted in
-    draw order.  Returns the cell-centred eps_rel array (nx, ny, nz), float64.
+    Boxes from ``box_specs_3d``, painted in draw order (later boxes win) by the
+    point-sampling rule at cell centres.  Returns the cell-centred eps_rel array
+    (nx, ny, nz), float64.
     """
-    rng = np.random.default_rng(seed)
     nx, ny, nz = dims
     eps = np.full((nx, ny, nz), float(background))
-    for _ in range(nboxes):
-        c = rng.uniform(0.0, 1.0, size=3) * np.array([nx, ny, nz])
-        e = rng.integers(edge[0], edge[1] + 1, size=3)
-        v = rng.uniform(*eps_range)
+    for c, e, v in box_specs_3d(dims, nboxes, seed, edge, eps_range):
         mx = _axis_mask(nx, c[0], e[0])
         my = _axis_mask(ny, c[1], e[1])
         mz = _axis_mask(nz, c[2], e[2])

@@ -1,8 +1,8 @@
 """Generate golden fixtures by running the reference Prismo package itself.
 
-Run in a checkout that has the reference source at /root/reference (read-only):
+Run with the path of a checkout of the reference project (read-only):
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py REFERENCE_CHECKOUT
 
 The reference is imported through a harness shim that changes no reference
 file: ``builtins.MTLBuffer`` is defined (backends/metal_backend.py:85 annotates
@@ -216,7 +216,9 @@ def scalar_fixture(prismo, name):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: make_golden.py REFERENCE_CHECKOUT")
+    root = sys.argv[1]
     prismo = import_reference(root)
     stepper_fixture(prismo, "ref_l0_3d.npz", (0.9e-6, 0.7e-6, 0.6e-6), 1e7, 2, 10, seed=1, lossy=True)
     stepper_fixture(prismo, "ref_l0_2d.npz", (1.7e-6, 1.3e-6, 0.0), 1e7, 3, 12, seed=2, lossy=True)

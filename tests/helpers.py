@@ -7,9 +7,10 @@ import numpy as np
 import pytest
 
 # the reference package: an installed copy under baseline/_ref (travels with the
-# repository to GPU machines), or the source tree of a local checkout (CPU tests)
+# repository to GPU machines), or a source tree named by PRISMO_REFERENCE_SRC (the
+# directory holding the ``prismo`` package); tests that need it skip without both
 INSTALLED = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "baseline", "_ref")
-SOURCE_TREES = [os.environ.get("PRISMO_REFERENCE_SRC", ""), "/root/reference/src"]
+SOURCE_TREES = [os.environ.get("PRISMO_REFERENCE_SRC", ""), INSTALLED]
 
 
 def import_reference(candidates):

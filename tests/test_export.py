@@ -9,11 +9,12 @@ from types import SimpleNamespace
 import numpy as np
 import pytest
 
+from helpers import SOURCE_TREES
 from prismo_gb300 import export as X
 
 
 def _reference_sparameters():
-    for root in (os.environ.get("PRISMO_REFERENCE_SRC", ""), "/root/reference/src"):
+    for root in SOURCE_TREES:
         p = os.path.join(root, "prismo", "analysis", "sparameters.py") if root else ""
         if p and os.path.exists(p):
             spec = importlib.util.spec_from_file_location("_ref_sparameters", p)

@@ -7,6 +7,7 @@ import os
 import numpy as np
 import pytest
 
+from helpers import SOURCE_TREES
 from oracle import fdtd64 as O
 
 
@@ -176,7 +177,7 @@ def _reference_mode_matching():
     """utils/mode_matching.py of the reference when its source tree is present."""
     import importlib.util
 
-    for root in (os.environ.get("PRISMO_REFERENCE_SRC", ""), "/root/reference/src"):
+    for root in SOURCE_TREES:
         p = os.path.join(root, "prismo", "utils", "mode_matching.py") if root else ""
         if p and os.path.exists(p):
             import sys
