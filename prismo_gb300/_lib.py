@@ -162,6 +162,7 @@ SIGNATURES = {
     "pc_batch_dft_flush": (C.c_int, [C.c_void_p, C.c_void_p]),
     "pc_batch_current_set": (C.c_int, [C.c_void_p]),
     "pc_batch_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p]),
+    "pc_batch_instance_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.c_void_p]),
     "pc_batch_launch_count": (C.c_int64, [C.c_void_p]),
     "pc_batch_steps_done": (C.c_int64, [C.c_void_p]),
     "pc_batch_destroy": (None, [C.c_void_p]),

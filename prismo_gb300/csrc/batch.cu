@@ -72,7 +72,18 @@ struct BPass {
     int npts;
     const double* w;  // source weights
     int live;         // 0: dry pass (no source, no sampling) used by the tuner
+    unsigned* status;       // batch status word
+    unsigned* inst_status;  // [ninst] per-instance status words
 };
+
+// Non-finite sentinel of one item: `chk` is the sum of the Ez values this thread
+// stored; NaN or Inf marks the item's instance (and the batch) failed.
+__device__ __forceinline__ void flag_nonfinite(const BPass& P, int inst, float chk) {
+    if (!isfinite(chk)) {
+        atomicOr(P.inst_status + inst, PC_STATUS_NONFINITE);
+        atomicOr(P.status, PC_STATUS_NONFINITE);
+    }
+}
 
 enum : unsigned {
     F_HX = 1u,
@@ -236,6 +247,7 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                 }
                 __syncthreads();
             }
+            float chk = 0.f;
 #pragma unroll
             for (int m = 0; m < MP; ++m) {
                 const int q = tid + m * BNT;
@@ -249,6 +261,7 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                     *reinterpret_cast<float2*>(fout + o) = er[m];
                     *reinterpret_cast<float2*>(fout + nxp + o) = xr[m];
                     *reinterpret_cast<float2*>(fout + 2 * nxp + o) = yr[m];
+                    chk += er[m].x + er[m].y;
                 } else {
                     const float ev[2] = {er[m].x, er[m].y}, xv[2] = {xr[m].x, xr[m].y}, yv[2] = {yr[m].x, yr[m].y};
 #pragma unroll
@@ -257,9 +270,11 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                         fout[o + h] = ev[h];
                         fout[nxp + o + h] = xv[h];
                         fout[2 * nxp + o + h] = yv[h];
+                        chk += ev[h];
                     }
                 }
             }
+            flag_nonfinite(P, it.x, chk);
             continue;
         }
         const int64_t pyx = sI.p_off;                      // psi Hy (x-derivative), [2t][pitch]
@@ -437,6 +452,7 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                 }
                 __syncthreads();
             }
+            float chk = 0.f;
 #pragma unroll
             for (int m = 0; m < MP; ++m) {
                 const int q = tid + m * BNT;
@@ -449,6 +465,7 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                     if (!(f & 8u)) continue;
                     const int gj = gy0 + (idx + h - (idx / RY) * RY);
                     const int64_t o = (int64_t)gi * pitch + gj;
+                    chk += h ? er[m].y : er[m].x;
                     fout[o] = h ? er[m].y : er[m].x;
                     fout[nxp + o] = h ? xr[m].y : xr[m].x;
                     fout[2 * nxp + o] = h ? yr[m].y : yr[m].x;
@@ -463,6 +480,7 @@ __global__ void __launch_bounds__(BNT, FAST ? BShape<TX, TY, K>::MINB_FAST : BSh
                     }
                 }
             }
+            flag_nonfinite(P, it.x, chk);
             continue;
         }
     }
@@ -514,6 +532,7 @@ struct pc_batch {
     int namps = 0;
     long long* d_step = nullptr;
     unsigned* d_status = nullptr;
+    unsigned* d_inst_status = nullptr;  // [ninst]
     float* set[2] = {nullptr, nullptr};
     float* cb = nullptr;
     float* psi[2] = {nullptr, nullptr};
@@ -655,6 +674,8 @@ BPass make_pass(pc_batch* b, int s_off, int row0, bool live) {
     P.npts = b->have_dft ? b->dft.npts : 0;
     P.w = b->d_w;
     P.live = live ? 1 : 0;
+    P.status = b->d_status;
+    P.inst_status = b->d_inst_status;
     return P;
 }
 
@@ -824,11 +845,13 @@ int pc_batch_create(int32_t ninst, const pc_batch_instance* desc, int32_t cpml_t
     bool ok = cudaMalloc(&b->d_inst, ninst * sizeof(BInst)) == cudaSuccess &&
               cudaMalloc(&b->d_step, sizeof(long long)) == cudaSuccess &&
               cudaMalloc(&b->d_status, sizeof(unsigned)) == cudaSuccess &&
+              cudaMalloc(&b->d_inst_status, ninst * sizeof(unsigned)) == cudaSuccess &&
               cudaMalloc(&b->d_w, std::max<int64_t>(woff, 1) * sizeof(double)) == cudaSuccess &&
               cudaMalloc(&b->d_slab, std::max(1, 6 * cpml_t) * sizeof(float)) == cudaSuccess;
     ok = ok && cudaMemcpy(b->d_inst, b->inst.data(), ninst * sizeof(BInst), cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemset(b->d_step, 0, sizeof(long long)) == cudaSuccess &&
          cudaMemset(b->d_status, 0, sizeof(unsigned)) == cudaSuccess &&
+         cudaMemset(b->d_inst_status, 0, ninst * sizeof(unsigned)) == cudaSuccess &&
          cudaMemset(b->d_w, 0, std::max<int64_t>(woff, 1) * sizeof(double)) == cudaSuccess;
     if (!ok) {
         pc_batch_destroy(b);
@@ -1046,6 +1069,16 @@ int pc_batch_status(pc_batch* b, uint32_t* flags, void* stream) {
     return PC_OK;
 }
 
+int pc_batch_instance_status(pc_batch* b, uint32_t* flags, void* stream) {
+    if (!b || !flags) return PC_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    static_assert(sizeof(unsigned) == sizeof(uint32_t), "status word size");
+    PC_CUDA_CHECK(cudaMemcpyAsync(flags, b->d_inst_status, b->ninst * sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    PC_CUDA_CHECK(cudaMemsetAsync(b->d_inst_status, 0, b->ninst * sizeof(unsigned), s));
+    PC_CUDA_CHECK(cudaStreamSynchronize(s));
+    return PC_OK;
+}
+
 int64_t pc_batch_launch_count(const pc_batch* b) { return b ? b->launches : PC_ERR_INVALID; }
 
 int64_t pc_batch_steps_done(const pc_batch* b) { return b ? b->steps_done : PC_ERR_INVALID; }
@@ -1061,6 +1094,7 @@ void pc_batch_destroy(pc_batch* b) {
     cudaFree(b->d_amps);
     cudaFree(b->d_step);
     cudaFree(b->d_status);
+    cudaFree(b->d_inst_status);
     cudaFree(b->d_items);
     delete b;
 }

@@ -9,7 +9,8 @@
 // with backward differences of E and forward differences of H.  These are the
 // reference curls (core/solver.py:167-309) with H written one index later, which
 // makes the discrete curl pair adjoint; psi <- b psi + a d is the Roden-Gedney
-// recursion with the boundaries/pml.py:117-257 profiles.
+// recursion with the boundaries/pml.py:117-257 profiles.  The E passes set
+// PC_STATUS_NONFINITE in the status word when a value they write is NaN or Inf.
 #include "pc_internal.cuh"
 #include "stencil_common.cuh"
 
@@ -69,6 +70,7 @@ __global__ void __launch_bounds__(256) split_e3(FieldArgs<T> a, CpmlArgs<T> p, A
     const T *Hx = a.Hin[0], *Hy = a.Hin[1], *Hz = a.Hin[2];
     T *Ex = a.Eout[0], *Ey = a.Eout[1], *Ez = a.Eout[2];
     const Idx3 q{i, j, k, nx, ny, nz, a.pitch};
+    T chk = T(0);  // non-finite sentinel: the sum of the values this thread wrote
     if (j < ny - 1 && k < nz - 1) {
         T c1 = (Hz[o + P] - Hz[o]) * a.inv_dy;
         T c2 = (Hy[o + 1] - Hy[o]) * a.inv_dz;
@@ -79,6 +81,7 @@ __global__ void __launch_bounds__(256) split_e3(FieldArgs<T> a, CpmlArgs<T> p, A
         T e = Ex[o];
         if (!(ADE && ade_update(ade, 0, i, j, k, c1 - c2, e))) e = ecoef(a.ca[0], o) * e + a.cb[0][o] * (c1 - c2);
         Ex[o] = e;
+        chk += e;
     }
     if (i < nx - 1 && k < nz - 1) {
         T c1 = (Hx[o + 1] - Hx[o]) * a.inv_dz;
@@ -90,6 +93,7 @@ __global__ void __launch_bounds__(256) split_e3(FieldArgs<T> a, CpmlArgs<T> p, A
         T e = Ey[o];
         if (!(ADE && ade_update(ade, 1, i, j, k, c1 - c2, e))) e = ecoef(a.ca[1], o) * e + a.cb[1][o] * (c1 - c2);
         Ey[o] = e;
+        chk += e;
     }
     if (i < nx - 1 && j < ny - 1) {
         T c1 = (Hy[o + R] - Hy[o]) * a.inv_dx;
@@ -101,7 +105,9 @@ __global__ void __launch_bounds__(256) split_e3(FieldArgs<T> a, CpmlArgs<T> p, A
         T e = Ez[o];
         if (!(ADE && ade_update(ade, 2, i, j, k, c1 - c2, e))) e = ecoef(a.ca[2], o) * e + a.cb[2][o] * (c1 - c2);
         Ez[o] = e;
+        chk += e;
     }
+    if (!isfinite(chk)) atomicOr(a.status, PC_STATUS_NONFINITE);
 }
 
 // 2D: both families (Ez, Hx, Hy) and (Hz, Ex, Ey); layout i * pitch + j.
@@ -148,6 +154,7 @@ __global__ void __launch_bounds__(256) split_e2(FieldArgs<T> a, CpmlArgs<T> p, A
     const T *Hx = a.Hin[0], *Hy = a.Hin[1], *Hz = a.Hin[2];
     T *Ex = a.Eout[0], *Ey = a.Eout[1], *Ez = a.Eout[2];
     const Idx2 q{i, j, nx, ny, a.pitch};
+    T chk = T(0);  // non-finite sentinel: the sum of the values this thread wrote
     if (i < nx - 1 && j < ny - 1) {
         T c1 = (Hy[o + P] - Hy[o]) * a.inv_dx;
         T c2 = (Hx[o + 1] - Hx[o]) * a.inv_dy;
@@ -158,6 +165,7 @@ __global__ void __launch_bounds__(256) split_e2(FieldArgs<T> a, CpmlArgs<T> p, A
         T e = Ez[o];
         if (!(ADE && ade_update(ade, 2, i, j, 0, c1 - c2, e))) e = ecoef(a.ca[2], o) * e + a.cb[2][o] * (c1 - c2);
         Ez[o] = e;
+        chk += e;
     }
     if (j < ny - 1) {
         T c = (Hz[o + 1] - Hz[o]) * a.inv_dy;
@@ -165,6 +173,7 @@ __global__ void __launch_bounds__(256) split_e2(FieldArgs<T> a, CpmlArgs<T> p, A
         T e = Ex[o];
         if (!(ADE && ade_update(ade, 0, i, j, 0, c, e))) e = ecoef(a.ca[0], o) * e + a.cb[0][o] * c;
         Ex[o] = e;
+        chk += e;
     }
     if (i < nx - 1) {
         T c = (Hz[o + P] - Hz[o]) * a.inv_dx;
@@ -172,7 +181,9 @@ __global__ void __launch_bounds__(256) split_e2(FieldArgs<T> a, CpmlArgs<T> p, A
         T e = Ey[o];
         if (!(ADE && ade_update(ade, 1, i, j, 0, -c, e))) e = ecoef(a.ca[1], o) * e - a.cb[1][o] * c;
         Ey[o] = e;
+        chk += e;
     }
+    if (!isfinite(chk)) atomicOr(a.status, PC_STATUS_NONFINITE);
 }
 
 template <typename T>

@@ -45,7 +45,7 @@ import ctypes as C
 import math
 import time
 from dataclasses import dataclass, field
-from typing import List, Optional, Sequence
+from typing import Callable, List, Optional, Sequence
 
 import numpy as np
 
@@ -459,6 +459,14 @@ class BatchedFDTD2D:
     def cur(self) -> int:
         return int(self.lib.pc_batch_current_set(self.h))
 
+    def instance_status(self) -> np.ndarray:
+        """Per-instance PC_STATUS_* words since the last read (then cleared):
+        PC_STATUS_NONFINITE marks an instance whose Ez became NaN or Inf."""
+        out = np.zeros(len(self.instances), dtype=np.uint32)
+        _lib.check(self.lib.pc_batch_instance_status(self.h, out.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                                     self.stream.cuda_stream), "pc_batch_instance_status")
+        return out
+
     # -- results ------------------------------------------------------------------
     def spectra(self):
         """Per instance, per port: complex128 (nf, n) DFT of Ez on the port line."""
@@ -506,6 +514,8 @@ class SweepResult:
     launches: int = 0
     variant: int = -1
     run_seconds: float = 0.0
+    rerun: List[int] = field(default_factory=list)   # designs re-run on the per-simulation path
+    failed: List[int] = field(default_factory=list)  # designs that failed there too (S is NaN)
 
     @property
     def designs_per_s(self) -> float:
@@ -513,11 +523,18 @@ class SweepResult:
 
 
 def batched_sweep(designs: Sequence[CouplerDesign], nsteps: int = STEPS, nfreq: int = NFREQ, device=None,
-                  autotune: bool = True, layouts=None, variant: Optional[int] = None) -> SweepResult:
+                  autotune: bool = True, layouts=None, variant: Optional[int] = None,
+                  prepare: Optional[Callable[["BatchedFDTD2D"], None]] = None) -> SweepResult:
     """S-parameters of every design from one batched run (couplers + normalisations).
 
     ``seconds`` runs from the design list to the S-parameters (layouts, device
-    setup, time loop, spectra); ``run_seconds`` is the time loop and spectra."""
+    setup, time loop, spectra); ``run_seconds`` is the time loop and spectra.
+    ``prepare`` (optional) is called with the batch before the time loop, e.g. to
+    seed initial fields.  A design whose coupler or normalisation instance ends
+    with a non-finite field is re-run on the per-simulation path
+    (``serial_sweep``) and listed in ``rerun``; if it fails there as well its
+    S-parameters are NaN and it is listed in ``failed`` (the reference's sweep
+    marks such a point as an error and goes on, optimization/sweep.py:183-195)."""
     import torch
 
     dev = torch.device(device or "cuda")
@@ -527,17 +544,30 @@ def batched_sweep(designs: Sequence[CouplerDesign], nsteps: int = STEPS, nfreq: 
     freqs = sweep_freqs(nfreq)
     B = BatchedFDTD2D(instances_for(layouts), freqs, device=dev, autotune=autotune, variant=variant)
     try:
+        if prepare is not None:
+            prepare(B)
         torch.cuda.synchronize(B.device)
         l0 = B.launches
         t1 = time.perf_counter()
         B.run(nsteps)
         spec = B.spectra()
+        st = B.instance_status()
         t2 = time.perf_counter()
-        S = np.stack([s_parameters(spec[2 * q], spec[2 * q + 1][0], L) for q, L in enumerate(layouts)])
+        bad = [q for q in range(len(layouts)) if (st[2 * q] | st[2 * q + 1]) & _lib.PC_STATUS_NONFINITE]
+        S = np.stack([s_parameters(spec[2 * q], spec[2 * q + 1][0], L) if q not in bad
+                      else np.full((4, len(freqs)), np.nan + 0j) for q, L in enumerate(layouts)])
+        failed = []
+        for q in bad:
+            try:
+                S[q] = serial_sweep([designs[q]], nsteps=nsteps, nfreq=nfreq, device=dev, layouts=[layouts[q]],
+                                    warm=False).S[0]
+            except FloatingPointError:
+                failed.append(q)
         t3 = time.perf_counter()
         cells = sum(I.eps.shape[0] * I.eps.shape[1] for I in B.instances) * nsteps
         r = SweepResult(list(designs), list(layouts), S, t3 - t0, cells, B.launches - l0, B.tuning()[0])
         r.run_seconds = t2 - t1
+        r.rerun, r.failed = bad, failed
         return r
     finally:
         B.close()
@@ -577,6 +607,11 @@ def serial_sweep(designs: Sequence[CouplerDesign], nsteps: int = STEPS, nfreq: i
                 pidx = (np.array([[p.x]]), np.arange(p.y0, p.y0 + p.n)[None, :])
                 ids.append(eng.add_dft("Ez", eng.offsets("Ez", pidx), freqs, dt))
             eng.step(nsteps, amps)
+            try:
+                eng.check_status()
+            except FloatingPointError:
+                eng.close()
+                raise
             spec.append([eng.dft_result(m).cpu().numpy().reshape(len(freqs), -1) for m in ids])
             launches += eng.launch_count()
             cells += nx * ny * nsteps
