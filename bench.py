@@ -254,6 +254,9 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--chunk", default=None,
                     help="x-chunk lengths 'CX[,EDGE]' of the fused schedule instead of autotuning (profiling runs)")
+    ap.add_argument("--time-blocking", type=int, default=0, choices=[0, 1, 2],
+                    help="time steps per launch of the temporally blocked stepper (0: the one-step fused schedule)")
+    ap.add_argument("--ts-chunk", type=int, default=0, help="x-chunk of the temporally blocked stepper (0: auto)")
     ap.add_argument("--dims", type=int, default=None,
                     help="cube edge for a reduced profiling case (default: the 256^3 workload)")
     ap.add_argument("--workload", default="3d", choices=["3d", "2d", "dispersive", "sweep", "surrogate", "mlp"],
@@ -294,6 +297,7 @@ def main():
         reset(eng)
         eng.step(tsteps, amps)
 
+    eng.set_time_blocking(args.time_blocking, args.ts_chunk)
     if args.chunk:
         cx, _, ce = args.chunk.partition(",")
         eng.set_chunk(int(cx), int(ce or 0))
@@ -322,7 +326,7 @@ def main():
     if ws > 1:
         torch.distributed.barrier()
     ms_total = ev0.elapsed_time(ev1)
-    kern_ms, kern_n = eng.profile_read()
+    kern_ms, kern_n, kern_steps = eng.profile_read()
     eng.profile(False)
     launches = eng.launch_count() - n0
     clk = clocks.stop()
@@ -606,7 +610,7 @@ def run_dispersive(args, peak, peak_kind):
     ev1.record(eng.stream)
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
-    kern_ms, kern_n = eng.profile_read()
+    kern_ms, kern_n, _ = eng.profile_read()
     clk = clocks.stop()
     status = eng.check_status()
     cells = float(np.prod(dims))

@@ -247,12 +247,19 @@ int64_t pc_launch_count(const pc_ctx* ctx);
  * its time loop from a CUDA graph of this many steps (a multiple of 16; 0 = one
  * launch sequence per step), captured on first use after an eager step and
  * re-captured after any call that changes what a step launches.  Steps with a
- * TFSF source or with pc_profile enabled always run eagerly.  Default 64. */
+ * TFSF source or with pc_profile enabled always run eagerly.  Default 64.
+ * PC_TUNE_TS_STEPS: time steps per launch of the temporally blocked 3D stepper
+ * (float32, lossless non-magnetic media, CPML, soft E sources fused in): 2
+ * advances two steps per launch wherever no monitor samples the intermediate
+ * step, 1 one step per launch, 0 (default) leaves it off (the fused schedule
+ * above runs).  PC_TUNE_TS_CHUNK: its x-chunk length (0 = automatic). */
 #define PC_TUNE_FUSED_CHUNK 1
 #define PC_TUNE_GRAPH_STEPS 2
 #define PC_TUNE_FUSED_CHUNK_EDGE 3
 #define PC_TUNE_FUSED_SPLIT 4
 #define PC_TUNE_FUSED_UNIFIED 5
+#define PC_TUNE_TS_STEPS 6
+#define PC_TUNE_TS_CHUNK 7
 int pc_set_tuning(pc_ctx* ctx, int32_t key, int64_t value);
 int64_t pc_get_tuning(const pc_ctx* ctx, int32_t key);
 
@@ -261,6 +268,10 @@ int64_t pc_get_tuning(const pc_ctx* ctx, int32_t key);
  * number of timed launches since the last read (synchronises the events). */
 int pc_profile(pc_ctx* ctx, int32_t enable);
 int pc_profile_read(pc_ctx* ctx, double* total_ms, int64_t* count);
+/* Time steps covered by the launches timed since the last pc_profile_read (a
+ * launch of the temporally blocked stepper covers two); read it before
+ * pc_profile_read, which resets it. */
+int64_t pc_profile_steps(const pc_ctx* ctx);
 
 /* Allocation-free stepping.  This entry point has no counterpart in the
  * reference; it serves callers that may not allocate device memory: a host

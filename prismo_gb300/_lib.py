@@ -36,6 +36,8 @@ PC_TUNE_FUSED_CHUNK_EDGE = 3
 PC_TUNE_FUSED_SPLIT = 4
 PC_TUNE_FUSED_UNIFIED = 5
 PC_TUNE_GRAPH_STEPS = 2
+PC_TUNE_TS_STEPS = 6
+PC_TUNE_TS_CHUNK = 7
 
 
 class GridDesc(C.Structure):
@@ -144,6 +146,7 @@ SIGNATURES = {
                                          C.POINTER(C.c_uint32)]),
     "pc_profile": (C.c_int, [C.c_void_p, C.c_int32]),
     "pc_profile_read": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    "pc_profile_steps": (C.c_int64, [C.c_void_p]),
     "pc_batch_create": (C.c_int, [C.c_int32, C.POINTER(BatchInstance), C.c_int32, C.c_double, C.c_double, C.c_double,
                                   C.c_double, C.POINTER(C.c_void_p), C.POINTER(BatchLayout)]),
     "pc_batch_instance_offsets": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),

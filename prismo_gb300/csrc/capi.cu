@@ -125,6 +125,7 @@ int pc_create(const pc_grid_desc* desc, pc_ctx** out) {
     c->graph_steps = 64;
     c->fused_split = 2;
     c->fused_unified = 1;
+    c->ts_k = 0;  // temporally blocked stepper off until it is chosen (pc_set_tuning)
     c->graph_gen[0] = c->graph_gen[1] = 0;
     if (cudaMalloc(&c->d_status, 2 * sizeof(uint32_t)) != cudaSuccess) {
         delete c;
@@ -161,6 +162,7 @@ void pc_destroy(pc_ctx* c) {
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     cudaFree(c->d_amps_g);
     destroy_fused_state(c);
+    destroy_ts_state(c);
     delete c;
 }
 
@@ -311,6 +313,8 @@ int pc_add_source(pc_ctx* c, int32_t comp, const int64_t* offsets, const double*
         cudaFree(d.d_w);
         return PC_ERR_CUDA;
     }
+    d.h_off.assign(offsets, offsets + n);
+    d.h_w = w;
     c->sources.push_back(d);
     return (int)c->sources.size() - 1;
 }
@@ -318,9 +322,11 @@ int pc_add_source(pc_ctx* c, int32_t comp, const int64_t* offsets, const double*
 namespace pc {
 namespace {
 
-// One leap-frog step n of a pc_step call: stencil, sources (amplitude row n of
+// Steps n (and n + 1) of a pc_step call: stencil, sources (amplitude rows of
 // c->d_amps), DFT sampling.  tamp: host TFSF amplitude of the step (or null).
-int one_step(pc_ctx* c, int n, const double* tamp, cudaStream_t s) {
+// Advances by two time steps in one launch of the temporally blocked stepper when
+// it applies and `left` allows; returns the number of steps taken (or < 0).
+int advance(pc_ctx* c, int n, int left, const double* tamp, cudaStream_t s) {
     int rc;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     if (c->prof_on) {
@@ -336,16 +342,29 @@ int one_step(pc_ctx* c, int n, const double* tamp, cudaStream_t s) {
         c->prof_used += 2;
         PC_CUDA_CHECK(cudaEventRecord(ev0, s));
     }
-    if (c->g.mode == PC_MODE_LEGACY)
+    int k = 1;
+    bool fused_sources = false;
+    if (c->g.mode == PC_MODE_LEGACY) {
         rc = launch_legacy_step(c, s);
-    else if (c->g.sched == PC_SCHED_FUSED && c->ade_n == 0 && !c->tfsf.on)
+    } else if (left >= 2 && ts_two_step_ok(c)) {
+        k = 2;
+        rc = launch_ts_step(c, 2, n, s, &fused_sources);
+    } else if (ts_eligible(c)) {
+        rc = launch_ts_step(c, 1, n, s, &fused_sources);
+    } else if (c->g.sched == PC_SCHED_FUSED && c->ade_n == 0 && !c->tfsf.on) {
         rc = launch_fused_step(c, s);
-    else
+    } else {
         rc = launch_split_step(c, s, tamp);
+    }
     if (rc) return rc;
-    if (ev1) PC_CUDA_CHECK(cudaEventRecord(ev1, s));
-    rc = launch_sources(c, n, s);
-    if (rc) return rc;
+    if (ev1) {
+        PC_CUDA_CHECK(cudaEventRecord(ev1, s));
+        c->prof_steps += k;
+    }
+    if (!fused_sources) {
+        rc = launch_sources(c, n, s);
+        if (rc) return rc;
+    }
     if (!c->dfts.empty()) {
         rc = dft_after_step(c, s);
         if (rc) return rc;
@@ -358,7 +377,7 @@ int one_step(pc_ctx* c, int n, const double* tamp, cudaStream_t s) {
         rc = mode_after_step(c, s);
         if (rc) return rc;
     }
-    return PC_OK;
+    return k;
 }
 
 // The graph of G steps for the current set (captured on first use).  Sources read
@@ -388,7 +407,14 @@ int ensure_step_graph(pc_ctx* c, int G, size_t ns) {
     cudaGraph_t gr = nullptr;
     PC_CUDA_CHECK(cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
     int rc = PC_OK;
-    for (int n = 0; n < G && !rc; ++n) rc = one_step(c, n, nullptr, c->cap_stream);
+    for (int n = 0; n < G;) {
+        const int k = advance(c, n, G - n, nullptr, c->cap_stream);
+        if (k < 0) {
+            rc = k;
+            break;
+        }
+        n += k;
+    }
     const cudaError_t e = cudaStreamEndCapture(c->cap_stream, &gr);
     const int64_t nodes = c->launches - launches0;
     c->d_amps = amps0;
@@ -466,10 +492,12 @@ int pc_step(pc_ctx* c, int32_t nsteps, const double* amps, void* stream) {
             c->graph_steps = 0;  // capture is not possible here: stay eager
         }
         const double* tamp = c->tfsf.on ? &amps[(size_t)n * ncol + ns] : nullptr;
-        const int rc = one_step(c, n, tamp, s);
-        if (rc) return rc;
+        // eager steps: the first one of a configuration runs alone (first-launch
+        // setup) so that a captured graph never holds it
+        const int k = advance(c, n, c->warm_gen == c->gen ? nsteps - n : std::min(nsteps - n, 2), tamp, s);
+        if (k < 0) return k;
         c->warm_gen = c->gen;
-        ++n;
+        n += k;
     }
     return PC_OK;
 }
@@ -591,6 +619,14 @@ int pc_set_tuning(pc_ctx* c, int32_t key, int64_t value) {
             if (value < 0 || value % 16 != 0 || value > (1 << 20)) return PC_ERR_INVALID;
             c->graph_steps = (int)value;
             return PC_OK;
+        case PC_TUNE_TS_STEPS:
+            if (value < 0 || value > 2) return PC_ERR_INVALID;
+            c->ts_k = (int)value;
+            return PC_OK;
+        case PC_TUNE_TS_CHUNK:
+            if (value < 0 || value > c->g.nx) return PC_ERR_INVALID;
+            c->ts_cx = (int)value;
+            return PC_OK;
         default:
             return PC_ERR_INVALID;
     }
@@ -603,6 +639,8 @@ int64_t pc_get_tuning(const pc_ctx* c, int32_t key) {
     if (key == PC_TUNE_FUSED_SPLIT) return c->fused_split;
     if (key == PC_TUNE_FUSED_UNIFIED) return c->fused_unified;
     if (key == PC_TUNE_GRAPH_STEPS) return c->graph_steps;
+    if (key == PC_TUNE_TS_STEPS) return c->ts_k;
+    if (key == PC_TUNE_TS_CHUNK) return c->ts_cx;
     return PC_ERR_INVALID;
 }
 
@@ -610,6 +648,7 @@ int pc_profile(pc_ctx* c, int32_t enable) {
     if (!c) return PC_ERR_INVALID;
     c->prof_on = enable != 0;
     c->prof_used = 0;
+    c->prof_steps = 0;
     return PC_OK;
 }
 
@@ -625,7 +664,10 @@ int pc_profile_read(pc_ctx* c, double* total_ms, int64_t* count) {
     *total_ms = tot;
     *count = (int64_t)(c->prof_used / 2);
     c->prof_used = 0;
+    c->prof_steps = 0;
     return PC_OK;
 }
+
+int64_t pc_profile_steps(const pc_ctx* c) { return c ? c->prof_steps : PC_ERR_INVALID; }
 
 }  // extern "C"

@@ -1,6 +1,7 @@
 // Internal declarations shared by the libprismo_cuda translation units.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -24,6 +25,8 @@ struct SourceDesc {
     int n;
     int64_t* d_off;   // device offsets
     double* d_w;      // device weights (float64, converted in-kernel)
+    std::vector<int64_t> h_off;  // host copies (the fused-source table of stepper_ts.cu)
+    std::vector<double> h_w;
 };
 
 // One DFT monitor: samples of `comp` at `npts` element offsets, accumulated for
@@ -174,10 +177,15 @@ struct pc_ctx {
     int fused_cx_edge;  // x-chunk of tiles that touch a y or z slab (0: fused_cx)
     int fused_split;    // CPML item classes: 0 general only, 1 + single-axis, 2 + two-axis (default)
     int fused_unified;  // every class in one launch (1, default) or one launch per class (0)
+    // temporally blocked stepper (stepper_ts.cu): time steps per launch (0 = off), x-chunk
+    void* ts_state;
+    int ts_k;
+    int ts_cx;
     // optional CUDA-event timing of the main stencil launch of every step
     bool prof_on;
     std::vector<cudaEvent_t> prof_ev;  // start/stop pairs, recycled
     size_t prof_used;
+    int64_t prof_steps;  // time steps covered by the timed launches since the last read
     // status
     uint32_t* d_status;
     uint32_t* d_legacy_flags;
@@ -211,6 +219,11 @@ int launch_tfsf_e(pc_ctx* c, double amp, cudaStream_t s);
 int launch_sources(pc_ctx* c, int step_in_batch, cudaStream_t s);
 int launch_fused_step(pc_ctx* c, cudaStream_t s);
 void destroy_fused_state(pc_ctx* c);
+int make_map(CUtensorMap* m, const void* base, const pc_grid_desc& g, int bw, int bh);
+bool ts_eligible(const pc_ctx* c);
+bool ts_two_step_ok(pc_ctx* c);
+int launch_ts_step(pc_ctx* c, int k, int row, cudaStream_t s, bool* fused_sources);
+void destroy_ts_state(pc_ctx* c);
 int dft_after_step(pc_ctx* c, cudaStream_t s);
 int launch_dft_sample_f32(const float* field, DftMonitor& m, int row, cudaStream_t s);
 int launch_dft_flush_rows(DftMonitor& m, int rows, cudaStream_t s);

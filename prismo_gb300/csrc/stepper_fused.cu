@@ -522,6 +522,10 @@ EncodeFn get_encode() {
     return fn;
 }
 
+}  // namespace
+
+// A 3D tiled tensor map over one padded field array (k fastest, then j, then i)
+// with a box of bw x bh x 1 elements; loads outside the array fill zero.
 int make_map(CUtensorMap* m, const void* base, const pc_grid_desc& g, int bw, int bh) {
     EncodeFn enc = get_encode();
     if (!enc) return PC_ERR_CUDA;
@@ -537,6 +541,7 @@ int make_map(CUtensorMap* m, const void* base, const pc_grid_desc& g, int bw, in
     return r == CUDA_SUCCESS ? PC_OK : PC_ERR_CUDA;
 }
 
+namespace {
 
 struct FusedState {
     const void* key_f[2][6];

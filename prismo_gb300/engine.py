@@ -425,11 +425,24 @@ class FDTDEngine:
         _lib.check(self.lib.pc_profile(self.ctx, 1 if enable else 0), "pc_profile")
 
     def profile_read(self):
-        """(summed ms, launches) of the main stencil kernel since the last read."""
+        """(summed ms, launches, time steps) of the main stencil kernel since the
+        last read (a launch of the temporally blocked stepper covers two steps)."""
         ms = C.c_double(0)
         n = C.c_int64(0)
+        steps = int(self.lib.pc_profile_steps(self.ctx))
         _lib.check(self.lib.pc_profile_read(self.ctx, C.byref(ms), C.byref(n)), "pc_profile_read")
-        return float(ms.value), int(n.value)
+        return float(ms.value), int(n.value), steps
+
+    def set_time_blocking(self, steps: int, chunk: int = 0):
+        """Time steps per launch of the temporally blocked 3D stepper (2: two steps
+        per launch wherever no monitor samples the step in between, 1: one, 0:
+        off, the fused schedule runs) and its x-chunk length (0: automatic)."""
+        _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_TS_STEPS, int(steps)), "pc_set_tuning")
+        _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_TS_CHUNK, int(chunk)), "pc_set_tuning")
+
+    def time_blocking(self):
+        return (int(self.lib.pc_get_tuning(self.ctx, _lib.PC_TUNE_TS_STEPS)),
+                int(self.lib.pc_get_tuning(self.ctx, _lib.PC_TUNE_TS_CHUNK)))
 
     # -- autotuning ---------------------------------------------------------------
     def autotune(self, candidates=(8, 16, 24, 32, 48, 64, 96), steps: int = 20, cache: bool = True):

@@ -201,6 +201,7 @@ def test_fused_chunking_with_cpml_slabs(torch, chunk):
     o.run(12)
     eng = make_engine(g.dims, g.spacing, dt, False, precision="fp32", sched="fused", material_arrays=mats,
                       pml=PMLParams(thickness=5))
+    eng.set_time_blocking(0)  # the fused schedule's own chunking
     if chunk:
         _lib.check(eng.lib.pc_set_tuning(eng.ctx, _lib.PC_TUNE_FUSED_CHUNK, chunk))
     load_fields(eng, init, torch)
@@ -236,6 +237,7 @@ def test_fused_plain_and_cpml_item_classes(torch, chunk, edge, split, unified):
     for prec in ("fp64", "fp32"):
         eng = make_engine(g.dims, g.spacing, dt, False, precision=prec, sched="fused", material_arrays=mats,
                           pml=PMLParams(thickness=8))
+        eng.set_time_blocking(0)  # the fused schedule's item classes
         if chunk:
             eng.set_chunk(chunk, edge)  # edge: chunk length of the tiles on a y/z slab
         eng.set_split(split, bool(unified))
