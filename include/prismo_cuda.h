@@ -250,9 +250,14 @@ int64_t pc_launch_count(const pc_ctx* ctx);
  * TFSF source or with pc_profile enabled always run eagerly.  Default 64.
  * PC_TUNE_TS_STEPS: time steps per launch of the temporally blocked 3D stepper
  * (float32, lossless non-magnetic media, CPML, soft E sources fused in): 2
- * advances two steps per launch wherever no monitor samples the intermediate
- * step, 1 one step per launch, 0 (default) leaves it off (the fused schedule
- * above runs).  PC_TUNE_TS_CHUNK: its x-chunk length (0 = automatic). */
+ * (default) advances two steps per launch wherever no monitor samples the
+ * intermediate step, 1 one step per launch, 0 leaves it off (the fused schedule
+ * above runs).  PC_TUNE_TS_CHUNK: its x-chunk length (0 = automatic, 32).
+ * PC_TUNE_TS_ORDER: its work-item order: 0 chunk after chunk in grid order, 1
+ * the most expensive chunks (those on the x slabs) first and the slower items
+ * of a chunk first, 2 (default) every item by its cost.  PC_TUNE_TS_ACTIVE
+ * (read only): 1 when the temporally blocked stepper runs for this context's
+ * current configuration. */
 #define PC_TUNE_FUSED_CHUNK 1
 #define PC_TUNE_GRAPH_STEPS 2
 #define PC_TUNE_FUSED_CHUNK_EDGE 3
@@ -260,6 +265,8 @@ int64_t pc_launch_count(const pc_ctx* ctx);
 #define PC_TUNE_FUSED_UNIFIED 5
 #define PC_TUNE_TS_STEPS 6
 #define PC_TUNE_TS_CHUNK 7
+#define PC_TUNE_TS_ORDER 8
+#define PC_TUNE_TS_ACTIVE 9
 int pc_set_tuning(pc_ctx* ctx, int32_t key, int64_t value);
 int64_t pc_get_tuning(const pc_ctx* ctx, int32_t key);
 

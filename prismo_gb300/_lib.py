@@ -38,6 +38,8 @@ PC_TUNE_FUSED_UNIFIED = 5
 PC_TUNE_GRAPH_STEPS = 2
 PC_TUNE_TS_STEPS = 6
 PC_TUNE_TS_CHUNK = 7
+PC_TUNE_TS_ORDER = 8
+PC_TUNE_TS_ACTIVE = 9
 
 
 class GridDesc(C.Structure):

@@ -125,7 +125,8 @@ int pc_create(const pc_grid_desc* desc, pc_ctx** out) {
     c->graph_steps = 64;
     c->fused_split = 2;
     c->fused_unified = 1;
-    c->ts_k = 0;  // temporally blocked stepper off until it is chosen (pc_set_tuning)
+    c->ts_k = 2;  // temporally blocked stepper where it applies (pc_set_tuning)
+    c->ts_order = 2;
     c->graph_gen[0] = c->graph_gen[1] = 0;
     if (cudaMalloc(&c->d_status, 2 * sizeof(uint32_t)) != cudaSuccess) {
         delete c;
@@ -627,6 +628,10 @@ int pc_set_tuning(pc_ctx* c, int32_t key, int64_t value) {
             if (value < 0 || value > c->g.nx) return PC_ERR_INVALID;
             c->ts_cx = (int)value;
             return PC_OK;
+        case PC_TUNE_TS_ORDER:
+            if (value < 0 || value > 2) return PC_ERR_INVALID;
+            c->ts_order = (int)value;
+            return PC_OK;
         default:
             return PC_ERR_INVALID;
     }
@@ -641,6 +646,8 @@ int64_t pc_get_tuning(const pc_ctx* c, int32_t key) {
     if (key == PC_TUNE_GRAPH_STEPS) return c->graph_steps;
     if (key == PC_TUNE_TS_STEPS) return c->ts_k;
     if (key == PC_TUNE_TS_CHUNK) return c->ts_cx;
+    if (key == PC_TUNE_TS_ORDER) return c->ts_order;
+    if (key == PC_TUNE_TS_ACTIVE) return ts_eligible(c) ? 1 : 0;
     return PC_ERR_INVALID;
 }
 

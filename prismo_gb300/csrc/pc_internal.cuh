@@ -181,6 +181,7 @@ struct pc_ctx {
     void* ts_state;
     int ts_k;
     int ts_cx;
+    int ts_order;  // work-item order (see PC_TUNE_TS_ORDER)
     // optional CUDA-event timing of the main stencil launch of every step
     bool prof_on;
     std::vector<cudaEvent_t> prof_ev;  // start/stop pairs, recycled

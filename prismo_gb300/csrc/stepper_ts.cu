@@ -88,10 +88,11 @@ enum { TC_PLAIN = 0, TC_EDGE = 1, TC_X = 2, TC_Y = 3, TC_Z = 4, TC_GEN = 5, TC_N
 template <int K>
 struct TsGeom {
     static constexpr int RJ = TS_TY + 2 * K;  // region rows: j in [j0-K, j0+TY+K)
-    static constexpr int RK = TS_TZ + 2 * K;  // region columns: k in [k0-K, k0+TZ+K)
-    static constexpr int CO = 4 - K;          // box column of region column 0
-    static constexpr int NPT = RJ * RK;
-    static constexpr int NT = (NPT + 31) / 32 * 32;
+    static constexpr int RK = TS_TZ + 4;      // region columns: k in [k0-2, k0+TZ+2) (pairs stay aligned)
+    static constexpr int CO = 2;              // box column of region column 0
+    static constexpr int NPR = RK / 2;        // k-pairs per region row
+    static constexpr int NPAIR = RJ * NPR;    // one pair of points per thread
+    static constexpr int NT = (NPAIR + 31) / 32 * 32;
     static constexpr int BOXF = RJ * TS_BW;  // floats of one box (one component, one plane)
     static constexpr int BOXB = (BOXF * 4 + 127) / 128 * 128;
     static constexpr int BQ = BOXB / 4;  // box stride in floats
@@ -122,29 +123,21 @@ struct P6 {
     float x0, x1, y0, y1, z0, z1;
 };
 
-// Per-thread constants of one region point.
-struct TsPt {
-    int si;                 // index in a box / buffer plane
-    int j, k;               // grid indices
-    bool act, own, kjd;     // region point, tile point owned by this CTA, inside the domain
+// Per-point constants (one of the two points a thread owns).
+struct TsPc {
+    int k;
+    bool kjd;                           // inside the domain
     bool mHx, mHy, mHz, mEx, mEy, mEz;  // j/k part of the update ranges
-    int64_t ojk;            // j * pitch + k (owned points)
-    int sy, sz;             // y / z slab index (-1: none)
-    float yb, ya, yk, zb, za, zk;
-    int oxc, oyc, ozc;      // plane-independent parts of the psi offsets
+    int sz;                             // z slab index (-1: none)
+    float zb, za, zk;
+    int oxc, oyc, ozc;                  // plane-independent parts of the psi offsets
 };
 
-__device__ __forceinline__ float psi_ld(const TsArgs& A, int o) {
-    if ((unsigned)o < (unsigned)A.psi_total) return __ldg(A.psi_in + o);
-    atomicOr(A.status, PC_STATUS_BOUNDS);
-    return 0.f;
-}
-__device__ __forceinline__ void psi_st(const TsArgs& A, int o, float v) {
-    if ((unsigned)o < (unsigned)A.psi_total)
-        A.psi_out[o] = v;
-    else
-        atomicOr(A.status, PC_STATUS_BOUNDS);
-}
+// Coefficients shared by the points of a row: y slab (index and b, a, kinv).
+struct TsRow {
+    int sy;
+    float yb, ya, yk;
+};
 
 // x-slab index of plane pl (-1: not a slab plane, or no x CPML in this variant)
 template <int AX>
@@ -153,26 +146,58 @@ __device__ __forceinline__ int x_slab(const TsArgs& A, int t, int pl) {
     return slab_of(pl, A.nx, t);
 }
 
-// psi of this point at plane pl (H slots if IS_H, else E slots); sx = x_slab(pl)
+// x-slab coefficients (b, a, kinv) of slab index sx (1, 0, 1 off the slabs)
+__device__ __forceinline__ void x_coef(const float* sC, int t2, int sx, float& b, float& a, float& kk) {
+    b = 1.f, a = 0.f, kk = 1.f;
+    if (sx >= 0) {
+        b = sC[sx];
+        a = sC[t2 + sx];
+        kk = sC[2 * t2 + sx];
+    }
+}
+
+// Plane part of the update ranges and the x-slab state of one plane (uniform).
+struct TsPlane {
+    bool hx, hi;  // H: plane in [0, nx-2] / [1, nx-2]
+    bool ed, ei;  // E: plane in [0, nx-1] / [0, nx-2]
+    int sx;       // x slab index (-1: none)
+    float xb, xa, xk;
+};
+
+template <int AX>
+__device__ __forceinline__ TsPlane plane_of(const TsArgs& A, const float* sC, int t, int pl) {
+    TsPlane P;
+    P.hx = pl >= 0 && pl <= A.nx - 2;
+    P.hi = pl >= 1 && pl <= A.nx - 2;
+    P.ed = pl >= 0 && pl <= A.nx - 1;
+    P.ei = P.hx;
+    P.sx = x_slab<AX>(A, t, pl);
+    x_coef(sC, 2 * t, P.sx, P.xb, P.xa, P.xk);
+    return P;
+}
+
+// psi of one point at plane pl (H slots if IS_H, else E slots); sx = x_slab(pl).
+// Offsets were range-checked once per work item (psi_ok).
 template <int AX, bool IS_H>
-__device__ __forceinline__ P6 psi_load(const TsArgs& A, const TsPt& pt, int t2, int pl, int sx) {
+__device__ __forceinline__ P6 psi_load(const TsArgs& A, const TsPc& pc, int sy, bool ok, int t2, int pl, int sx) {
     P6 v{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (AX == 0 || !pt.act || !pt.kjd || pl < 0 || pl >= A.nx) return v;
+    if (AX == 0 || !ok || !pc.kjd || pl < 0 || pl >= A.nx) return v;
     const int P32 = A.pitch, ny = A.ny;
+    const float* in = A.psi_in;
     if ((AX & 1) && sx >= 0) {
-        const int o = pt.oxc + sx * (ny * P32);
-        v.x0 = psi_ld(A, o + (IS_H ? SX_HY : SX_EY) * A.se[0]);
-        v.x1 = psi_ld(A, o + (IS_H ? SX_HZ : SX_EZ) * A.se[0]);
+        const int o = pc.oxc + sx * (ny * P32);
+        v.x0 = __ldg(in + o + (IS_H ? SX_HY : SX_EY) * A.se[0]);
+        v.x1 = __ldg(in + o + (IS_H ? SX_HZ : SX_EZ) * A.se[0]);
     }
-    if ((AX & 2) && pt.sy >= 0) {
-        const int o = pt.oyc + pl * (t2 * P32);
-        v.y0 = psi_ld(A, o + (IS_H ? SY_HX : SY_EX) * A.se[1]);
-        v.y1 = psi_ld(A, o + (IS_H ? SY_HZ : SY_EZ) * A.se[1]);
+    if ((AX & 2) && sy >= 0) {
+        const int o = pc.oyc + pl * (t2 * P32);
+        v.y0 = __ldg(in + o + (IS_H ? SY_HX : SY_EX) * A.se[1]);
+        v.y1 = __ldg(in + o + (IS_H ? SY_HZ : SY_EZ) * A.se[1]);
     }
-    if ((AX & 4) && pt.sz >= 0) {
-        const int o = pt.ozc + pl * (ny * t2);
-        v.z0 = psi_ld(A, o + (IS_H ? SZ_HX : SZ_EX) * A.se[2]);
-        v.z1 = psi_ld(A, o + (IS_H ? SZ_HY : SZ_EY) * A.se[2]);
+    if ((AX & 4) && pc.sz >= 0) {
+        const int o = pc.ozc + pl * (ny * t2);
+        v.z0 = __ldg(in + o + (IS_H ? SZ_HX : SZ_EX) * A.se[2]);
+        v.z1 = __ldg(in + o + (IS_H ? SZ_HY : SZ_EY) * A.se[2]);
     }
     return v;
 }
@@ -180,63 +205,66 @@ __device__ __forceinline__ P6 psi_load(const TsArgs& A, const TsPt& pt, int t2, 
 // the owner's psi at plane pl; u0/u1/u2: whether the x/y/z component of the field
 // was updated there (the psi of a component that is not updated is not stored)
 template <int AX, bool IS_H>
-__device__ __forceinline__ void psi_store(const TsArgs& A, const TsPt& pt, int t2, int pl, int sx, const P6& v,
-                                          bool u0, bool u1, bool u2) {
+__device__ __forceinline__ void psi_store(const TsArgs& A, const TsPc& pc, int sy, int t2, int pl, int sx,
+                                          const P6& v, bool u0, bool u1, bool u2) {
+    if (!pc.kjd) return;
     const int P32 = A.pitch, ny = A.ny;
+    float* out = A.psi_out;
     // slot -> component: H (Hy Hz | Hx Hz | Hx Hy), E (Ey Ez | Ex Ez | Ex Ey)
     if ((AX & 1) && sx >= 0) {
-        const int o = pt.oxc + sx * (ny * P32);
-        if (u1) psi_st(A, o + (IS_H ? SX_HY : SX_EY) * A.se[0], v.x0);
-        if (u2) psi_st(A, o + (IS_H ? SX_HZ : SX_EZ) * A.se[0], v.x1);
+        const int o = pc.oxc + sx * (ny * P32);
+        if (u1) out[o + (IS_H ? SX_HY : SX_EY) * A.se[0]] = v.x0;
+        if (u2) out[o + (IS_H ? SX_HZ : SX_EZ) * A.se[0]] = v.x1;
     }
-    if ((AX & 2) && pt.sy >= 0) {
-        const int o = pt.oyc + pl * (t2 * P32);
-        if (u0) psi_st(A, o + (IS_H ? SY_HX : SY_EX) * A.se[1], v.y0);
-        if (u2) psi_st(A, o + (IS_H ? SY_HZ : SY_EZ) * A.se[1], v.y1);
+    if ((AX & 2) && sy >= 0) {
+        const int o = pc.oyc + pl * (t2 * P32);
+        if (u0) out[o + (IS_H ? SY_HX : SY_EX) * A.se[1]] = v.y0;
+        if (u2) out[o + (IS_H ? SY_HZ : SY_EZ) * A.se[1]] = v.y1;
     }
-    if ((AX & 4) && pt.sz >= 0) {
-        const int o = pt.ozc + pl * (ny * t2);
-        if (u0) psi_st(A, o + (IS_H ? SZ_HX : SZ_EX) * A.se[2], v.z0);
-        if (u1) psi_st(A, o + (IS_H ? SZ_HY : SZ_EY) * A.se[2], v.z1);
+    if ((AX & 4) && pc.sz >= 0) {
+        const int o = pc.ozc + pl * (ny * t2);
+        if (u0) out[o + (IS_H ? SZ_HX : SZ_EX) * A.se[2]] = v.z0;
+        if (u1) out[o + (IS_H ? SZ_HY : SZ_EY) * A.se[2]] = v.z1;
     }
 }
 
-// H at plane p of this point from E(p) (planes e at stride bq: own value and the
-// j-1 / k-1 neighbours) and the point's own E(p-1) (emy, emz).  sx: the plane's x
-// slab index, xc: its (b, a, kinv) when sx >= 0.  u: components updated.
+// H at plane p of one point: own E(p) (ex, ey, ez), neighbours Ez, Ex at j-1 and
+// Ey, Ex at k-1, own E(p-1) (emy, emz).  px / pi: the plane lies in [0, nx-2] /
+// [1, nx-2]; use_psi: the point or the plane lies in a slab; sx / (xb, xa, xk):
+// the plane's x slab.
 template <int AX, bool MASK>
-__device__ __forceinline__ void h_upd(const TsArgs& A, const TsPt& pt, const float* e, int bq, float ex, float ey,
-                                      float ez, float emy, float emz, int p, int sx, float xb, float xa, float xk,
-                                      float& hx, float& hy, float& hz, P6& ps, bool& ux, bool& uy, bool& uz) {
-    constexpr int BW = TS_BW;
-    const int si = pt.si;
+__device__ __forceinline__ void h_point(const TsArgs& A, const TsPc& pc, const TsRow& rw, float ex, float ey, float ez,
+                                        float ezj, float exj, float eyk, float exk, float emy, float emz, bool px,
+                                        bool pi, bool use_psi, int sx, float xb, float xa, float xk, float& hx,
+                                        float& hy, float& hz, P6& ps, bool& ux, bool& uy, bool& uz) {
     float d0 = (ez - emz) * A.inv_dx;
     float d1 = (ey - emy) * A.inv_dx;
-    float d2 = (ez - e[2 * bq + si - BW]) * A.inv_dy;
-    float d3 = (ex - e[si - BW]) * A.inv_dy;
-    float d4 = (ey - e[bq + si - 1]) * A.inv_dz;
-    float d5 = (ex - e[si - 1]) * A.inv_dz;
-    if ((AX & 1) && sx >= 0 && pt.kjd) {
-        d0 = tstep(xb, xa, xk, d0, ps.x0);
-        d1 = tstep(xb, xa, xk, d1, ps.x1);
-    }
-    if ((AX & 2) && pt.sy >= 0) {
-        d2 = tstep(pt.yb, pt.ya, pt.yk, d2, ps.y0);
-        d3 = tstep(pt.yb, pt.ya, pt.yk, d3, ps.y1);
-    }
-    if ((AX & 4) && pt.sz >= 0) {
-        d4 = tstep(pt.zb, pt.za, pt.zk, d4, ps.z0);
-        d5 = tstep(pt.zb, pt.za, pt.zk, d5, ps.z1);
+    float d2 = (ez - ezj) * A.inv_dy;
+    float d3 = (ex - exj) * A.inv_dy;
+    float d4 = (ey - eyk) * A.inv_dz;
+    float d5 = (ex - exk) * A.inv_dz;
+    if (AX != 0 && use_psi) {
+        if ((AX & 1) && sx >= 0 && pc.kjd) {
+            d0 = tstep(xb, xa, xk, d0, ps.x0);
+            d1 = tstep(xb, xa, xk, d1, ps.x1);
+        }
+        if ((AX & 2) && rw.sy >= 0 && pc.kjd) {
+            d2 = tstep(rw.yb, rw.ya, rw.yk, d2, ps.y0);
+            d3 = tstep(rw.yb, rw.ya, rw.yk, d3, ps.y1);
+        }
+        if ((AX & 4) && pc.sz >= 0) {
+            d4 = tstep(pc.zb, pc.za, pc.zk, d4, ps.z0);
+            d5 = tstep(pc.zb, pc.za, pc.zk, d5, ps.z1);
+        }
     }
     const float db = A.db;
     const float nhx = hx - db * (d2 - d4);
     const float nhy = hy - db * (d5 - d0);
     const float nhz = hz - db * (d1 - d3);
     if (MASK) {
-        const bool px = p >= 0 && p <= A.nx - 2, pi = p >= 1 && p <= A.nx - 2;
-        ux = pt.mHx && px;
-        uy = pt.mHy && pi;
-        uz = pt.mHz && pi;
+        ux = pc.mHx && px;
+        uy = pc.mHy && pi;
+        uz = pc.mHz && pi;
         hx = ux ? nhx : hx;
         hy = uy ? nhy : hy;
         hz = uz ? nhz : hz;
@@ -248,41 +276,42 @@ __device__ __forceinline__ void h_upd(const TsArgs& A, const TsPt& pt, const flo
     }
 }
 
-// E at plane q of this point from H(q) (planes h at stride bq: the j+1 / k+1
-// neighbours), its own H(q) (hxq, hyq, hzq) and H(q+1) (hyn, hzn).
+// E at plane q of one point: neighbours Hz, Hx at j+1 and Hy, Hx at k+1, own H(q)
+// (hxq, hyq, hzq) and H(q+1) (hyn, hzn), Cb (cbx, cby, cbz).  qd / qi: the plane
+// lies in [0, nx-1] / [0, nx-2].
 template <int AX, bool MASK>
-__device__ __forceinline__ void e_upd(const TsArgs& A, const TsPt& pt, const float* h, int bq, float hxq, float hyq,
-                                      float hzq, float hyn, float hzn, int q, int sx, float xb, float xa, float xk,
-                                      float cbx, float cby, float cbz, float& ex, float& ey, float& ez, P6& ps,
-                                      bool& ux, bool& uy, bool& uz) {
-    constexpr int BW = TS_BW;
-    const int si = pt.si;
+__device__ __forceinline__ void e_point(const TsArgs& A, const TsPc& pc, const TsRow& rw, float hzj, float hxj,
+                                        float hyk, float hxk, float hxq, float hyq, float hzq, float hyn, float hzn,
+                                        bool qd, bool qi, bool use_psi, int sx, float xb, float xa, float xk,
+                                        float cbx, float cby, float cbz, float& ex, float& ey, float& ez, P6& ps,
+                                        bool& ux, bool& uy, bool& uz) {
     float d0 = (hzn - hzq) * A.inv_dx;
     float d1 = (hyn - hyq) * A.inv_dx;
-    float d2 = (h[2 * bq + si + BW] - hzq) * A.inv_dy;
-    float d3 = (h[si + BW] - hxq) * A.inv_dy;
-    float d4 = (h[bq + si + 1] - hyq) * A.inv_dz;
-    float d5 = (h[si + 1] - hxq) * A.inv_dz;
-    if ((AX & 1) && sx >= 0 && pt.kjd) {
-        d0 = tstep(xb, xa, xk, d0, ps.x0);
-        d1 = tstep(xb, xa, xk, d1, ps.x1);
-    }
-    if ((AX & 2) && pt.sy >= 0) {
-        d2 = tstep(pt.yb, pt.ya, pt.yk, d2, ps.y0);
-        d3 = tstep(pt.yb, pt.ya, pt.yk, d3, ps.y1);
-    }
-    if ((AX & 4) && pt.sz >= 0) {
-        d4 = tstep(pt.zb, pt.za, pt.zk, d4, ps.z0);
-        d5 = tstep(pt.zb, pt.za, pt.zk, d5, ps.z1);
+    float d2 = (hzj - hzq) * A.inv_dy;
+    float d3 = (hxj - hxq) * A.inv_dy;
+    float d4 = (hyk - hyq) * A.inv_dz;
+    float d5 = (hxk - hxq) * A.inv_dz;
+    if (AX != 0 && use_psi) {
+        if ((AX & 1) && sx >= 0 && pc.kjd) {
+            d0 = tstep(xb, xa, xk, d0, ps.x0);
+            d1 = tstep(xb, xa, xk, d1, ps.x1);
+        }
+        if ((AX & 2) && rw.sy >= 0 && pc.kjd) {
+            d2 = tstep(rw.yb, rw.ya, rw.yk, d2, ps.y0);
+            d3 = tstep(rw.yb, rw.ya, rw.yk, d3, ps.y1);
+        }
+        if ((AX & 4) && pc.sz >= 0) {
+            d4 = tstep(pc.zb, pc.za, pc.zk, d4, ps.z0);
+            d5 = tstep(pc.zb, pc.za, pc.zk, d5, ps.z1);
+        }
     }
     const float nex = ex + cbx * (d2 - d4);
     const float ney = ey + cby * (d5 - d0);
     const float nez = ez + cbz * (d1 - d3);
     if (MASK) {
-        const bool qd = q >= 0 && q <= A.nx - 1, qi = q >= 0 && q <= A.nx - 2;
-        ux = pt.mEx && qd;
-        uy = pt.mEy && qi;
-        uz = pt.mEz && qi;
+        ux = pc.mEx && qd;
+        uy = pc.mEy && qi;
+        uz = pc.mEz && qi;
         ex = ux ? nex : ex;
         ey = uy ? ney : ey;
         ez = uz ? nez : ez;
@@ -294,12 +323,12 @@ __device__ __forceinline__ void e_upd(const TsArgs& A, const TsPt& pt, const flo
     }
 }
 
-// fused soft sources of E at plane q, amplitude row `row` of the call
-__device__ __forceinline__ void add_src(const TsArgs& A, const TsPt& pt, int q, int row, float& ex, float& ey,
+// fused soft sources of E at plane q, point (j, k), amplitude row `row` of the call
+__device__ __forceinline__ void add_src(const TsArgs& A, int j, int k, int q, int row, float& ex, float& ey,
                                         float& ez) {
     for (int m = 0; m < A.nsrc; ++m) {
         const TsSrc S = A.src[m];
-        if (S.i == q && S.j == pt.j && S.k == pt.k) {
+        if (S.i == q && S.j == j && S.k == k) {
             const float v = static_cast<float>(S.w * A.amps[(size_t)row * A.ns + S.col]);
             if (S.comp == 0)
                 ex = ex + v;
@@ -311,13 +340,94 @@ __device__ __forceinline__ void add_src(const TsArgs& A, const TsPt& pt, int q, 
     }
 }
 
-// x-slab coefficients (b, a, kinv) of slab index sx (1, 0, 1 off the slabs)
-__device__ __forceinline__ void x_coef(const float* sC, int t2, int sx, float& b, float& a, float& kk) {
-    b = 1.f, a = 0.f, kk = 1.f;
-    if (sx >= 0) {
-        b = sC[sx];
-        a = sC[t2 + sx];
-        kk = sC[2 * t2 + sx];
+__device__ __forceinline__ float2 ld2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void st2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
+
+// Field values of a pair of points (.x: the point at k, .y: the one at k+1).
+struct V3 {
+    float2 x, y, z;
+};
+__device__ __forceinline__ V3 ld3(const float* b, int bq, int si) {
+    return V3{ld2(b + si), ld2(b + bq + si), ld2(b + 2 * bq + si)};
+}
+__device__ __forceinline__ void st3(float* b, int bq, int si, const V3& v) {
+    st2(b + si, v.x.x, v.x.y);
+    st2(b + bq + si, v.y.x, v.y.y);
+    st2(b + 2 * bq + si, v.z.x, v.z.y);
+}
+
+// H sub-step of a pair at plane P: E(p) planes e (own pair and neighbours), own
+// E(p-1) (em), H in/out (h).
+template <int AX, bool MASK>
+__device__ __forceinline__ void h_pair(const TsArgs& A, const TsPc* pc, const TsRow& rw, const float* e, int bq, int si,
+                                       const V3& eo, const V3& em, const TsPlane& P, bool use_psi, V3& h, P6* ps,
+                                       bool* u) {
+    constexpr int BW = TS_BW;
+    const float2 ezj = ld2(e + 2 * bq + si - BW), exj = ld2(e + si - BW);
+    const float eyk = e[bq + si - 1], exk = e[si - 1];
+    h_point<AX, MASK>(A, pc[0], rw, eo.x.x, eo.y.x, eo.z.x, ezj.x, exj.x, eyk, exk, em.y.x, em.z.x, P.hx, P.hi,
+                      use_psi, P.sx, P.xb, P.xa, P.xk, h.x.x, h.y.x, h.z.x, ps[0], u[0], u[1], u[2]);
+    h_point<AX, MASK>(A, pc[1], rw, eo.x.y, eo.y.y, eo.z.y, ezj.y, exj.y, eo.y.x, eo.x.x, em.y.y, em.z.y, P.hx, P.hi,
+                      use_psi, P.sx, P.xb, P.xa, P.xk, h.x.y, h.y.y, h.z.y, ps[1], u[3], u[4], u[5]);
+}
+
+// E sub-step of a pair at plane P: H(q) planes h (neighbours), own H(q) (hq) and
+// H(q+1) (hn), Cb (cb), E in/out (e).
+template <int AX, bool MASK>
+__device__ __forceinline__ void e_pair(const TsArgs& A, const TsPc* pc, const TsRow& rw, const float* h, int bq, int si,
+                                       const V3& hq, const V3& hn, const V3& cb, const TsPlane& P, bool use_psi, V3& e,
+                                       P6* ps, bool* u) {
+    constexpr int BW = TS_BW;
+    const float2 hzj = ld2(h + 2 * bq + si + BW), hxj = ld2(h + si + BW);
+    const float hyk = h[bq + si + 2], hxk = h[si + 2];
+    e_point<AX, MASK>(A, pc[0], rw, hzj.x, hxj.x, hq.y.y, hq.x.y, hq.x.x, hq.y.x, hq.z.x, hn.y.x, hn.z.x, P.ed, P.ei,
+                      use_psi, P.sx, P.xb, P.xa, P.xk, cb.x.x, cb.y.x, cb.z.x, e.x.x, e.y.x, e.z.x, ps[0], u[0], u[1],
+                      u[2]);
+    e_point<AX, MASK>(A, pc[1], rw, hzj.y, hxj.y, hyk, hxk, hq.x.y, hq.y.y, hq.z.y, hn.y.y, hn.z.y, P.ed, P.ei,
+                      use_psi, P.sx, P.xb, P.xa, P.xk, cb.x.y, cb.y.y, cb.z.y, e.x.y, e.y.y, e.z.y, ps[1], u[3], u[4],
+                      u[5]);
+}
+
+// Region row r and pair column u of thread `tid` (< RJ * NPR).  With z CPML in
+// the variant, the pair columns holding z-slab points come first, so that warps
+// hold either slab pairs or none and only the former run the z recursions.
+template <int K, int AX>
+__device__ __forceinline__ void pair_of(int tid, int k0, int nz, int t, int& r, int& u) {
+    constexpr int NPR = TsGeom<K>::NPR;
+    auto slab_pair = [&](int v) {
+        const int k = k0 - 2 + 2 * v;
+        const bool s0 = k >= 0 && k < nz && (k < t || k >= nz - t);
+        const bool s1 = k + 1 >= 0 && k + 1 < nz && (k + 1 < t || k + 1 >= nz - t);
+        return s0 || s1;
+    };
+    int ns = 0;
+    if (AX & 4)
+        for (int v = 0; v < NPR; ++v) ns += slab_pair(v) ? 1 : 0;
+    if (ns == 0 || ns == NPR) {
+        r = tid / NPR;
+        u = tid - r * NPR;
+        return;
+    }
+    const int rows_slab = TsGeom<K>::RJ * ns;
+    const bool want_slab = tid < rows_slab;
+    int want;
+    if (want_slab) {
+        r = tid / ns;
+        want = tid - r * ns;
+    } else {
+        const int v2 = tid - rows_slab, nn = NPR - ns;
+        r = v2 / nn;
+        want = v2 - r * nn;
+    }
+    u = 0;
+    for (int v = 0, seen = 0; v < NPR; ++v) {
+        if (slab_pair(v) == want_slab) {
+            if (seen == want) {
+                u = v;
+                break;
+            }
+            ++seen;
+        }
     }
 }
 
@@ -368,72 +478,105 @@ __device__ __forceinline__ void ts3_item(const TsArgs& A, const TsMaps& maps, co
     if (tid == 0)
         for (int n = 0; n < issued; ++n) issue(n);
 
-    // ---- this thread's region point -------------------------------------------
-    TsPt pt;
-    pt.act = tid < G::NPT;
-    {
-        const int r = pt.act ? tid / G::RK : 0;
-        const int c = pt.act ? tid - r * G::RK : 0;
-        pt.si = r * TS_BW + c + G::CO;
-        pt.j = j0 - K + r;
-        pt.k = k0 - K + c;
-        pt.own = pt.act && r >= K && r < K + TS_TY && c >= K && c < K + TS_TZ && pt.j < ny && pt.k < nz;
-    }
-    const int j = pt.j, k = pt.k;
+    // ---- this thread's pair of region points ----------------------------------
+    const bool act = tid < G::NPAIR;
+    int r = 0, u = 0;
+    if (act) pair_of<K, AX>(tid, k0, nz, t, r, u);
+    const int si = r * TS_BW + 2 * u + G::CO;  // even: float2 accesses stay aligned
+    const int j = j0 - K + r;
+    const int kp = k0 - 2 + 2 * u;  // the pair's first k (even when k0 is)
+    const bool own = act && r >= K && r < K + TS_TY && u >= 1 && u <= TS_TZ / 2 && j < ny && kp < nz;
     const int64_t PR = (int64_t)ny * A.pitch;
-    pt.ojk = pt.own ? (int64_t)j * A.pitch + k : 0;
-    pt.kjd = j >= 0 && j < ny && k >= 0 && k < nz;
-    // update ranges of the reference stepper (component shapes, core/grid.py:157-168;
-    // H interior, core/solver.py:167-253 with the corrected slices): the j/k parts
-    pt.mHx = pt.mHy = pt.mHz = pt.mEx = pt.mEy = pt.mEz = true;
-    if (MASK) {
-        const bool jd = j >= 0 && j < ny, kd = k >= 0 && k < nz;
-        const bool jin = j >= 1 && j <= ny - 2, kin = k >= 1 && k <= nz - 2;
-        pt.mHx = jin && kin;
-        pt.mHy = jd && j <= ny - 2 && kin;
-        pt.mHz = jin && kd && k <= nz - 2;
-        pt.mEx = jd && kd && j <= ny - 2 && k <= nz - 2;
-        pt.mEy = jd && kd && k <= nz - 2;
-        pt.mEz = jd && kd && j <= ny - 2;
-    }
-    pt.sy = pt.sz = -1;
-    pt.yb = pt.yk = pt.zb = pt.zk = 1.f;
-    pt.ya = pt.za = 0.f;
-    if ((AX & 2) && pt.kjd) {
-        pt.sy = slab_of(j, ny, t);
-        if (pt.sy >= 0) {
-            pt.yb = sC[3 * t2 + pt.sy];
-            pt.ya = sC[4 * t2 + pt.sy];
-            pt.yk = sC[5 * t2 + pt.sy];
+    const int64_t ojk = own ? (int64_t)j * A.pitch + kp : 0;
+    TsRow rw;
+    rw.sy = -1;
+    rw.yb = rw.yk = 1.f;
+    rw.ya = 0.f;
+    const bool jd = j >= 0 && j < ny;
+    if ((AX & 2) && jd) {
+        rw.sy = slab_of(j, ny, t);
+        if (rw.sy >= 0) {
+            rw.yb = sC[3 * t2 + rw.sy];
+            rw.ya = sC[4 * t2 + rw.sy];
+            rw.yk = sC[5 * t2 + rw.sy];
         }
     }
-    if ((AX & 4) && pt.kjd) {
-        pt.sz = slab_of(k, nz, t);
-        if (pt.sz >= 0) {
-            pt.zb = sC[6 * t2 + pt.sz];
-            pt.za = sC[7 * t2 + pt.sz];
-            pt.zk = sC[8 * t2 + pt.sz];
+    TsPc pc[2];
+    bool psi_ok = true;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        TsPc& c = pc[h];
+        const int k = kp + h;
+        c.k = k;
+        c.kjd = act && jd && k >= 0 && k < nz;
+        // update ranges of the reference stepper (component shapes, core/grid.py:157-168;
+        // H interior, core/solver.py:167-253 with the corrected slices): the j/k parts
+        c.mHx = c.mHy = c.mHz = c.mEx = c.mEy = c.mEz = true;
+        if (MASK) {
+            const bool kd = k >= 0 && k < nz;
+            const bool jin = j >= 1 && j <= ny - 2, kin = k >= 1 && k <= nz - 2;
+            c.mHx = jin && kin;
+            c.mHy = jd && j <= ny - 2 && kin;
+            c.mHz = jin && kd && k <= nz - 2;
+            c.mEx = jd && kd && j <= ny - 2 && k <= nz - 2;
+            c.mEy = jd && kd && k <= nz - 2;
+            c.mEz = jd && kd && j <= ny - 2;
         }
-    }
-    {
+        c.sz = -1;
+        c.zb = c.zk = 1.f;
+        c.za = 0.f;
+        if ((AX & 4) && c.kjd) {
+            c.sz = slab_of(k, nz, t);
+            if (c.sz >= 0) {
+                c.zb = sC[6 * t2 + c.sz];
+                c.za = sC[7 * t2 + c.sz];
+                c.zk = sC[8 * t2 + c.sz];
+            }
+        }
         const int P32 = A.pitch;
-        pt.oxc = A.ab[0] + j * P32 + k;
-        pt.oyc = A.ab[1] + (pt.sy >= 0 ? pt.sy : 0) * P32 + k;
-        pt.ozc = A.ab[2] + j * t2 + (pt.sz >= 0 ? pt.sz : 0);
+        c.oxc = A.ab[0] + j * P32 + k;
+        c.oyc = A.ab[1] + (rw.sy >= 0 ? rw.sy : 0) * P32 + k;
+        c.ozc = A.ab[2] + j * t2 + (c.sz >= 0 ? c.sz : 0);
+        if (CP && c.kjd) {
+            // every psi offset this point forms over the item's planes, checked once:
+            // x-slab entries at any slab index, y/z-slab entries up to the last plane
+            const int64_t last = min(ie + K, A.nx) - 1;
+            const int64_t tot = A.psi_total;
+            bool ok = true;
+            if (AX & 1) ok = ok && c.oxc >= 0 && (int64_t)c.oxc + (int64_t)(t2 - 1) * ny * P32 + 3LL * A.se[0] < tot;
+            if ((AX & 2) && rw.sy >= 0) ok = ok && c.oyc >= 0 && (int64_t)c.oyc + last * t2 * P32 + 3LL * A.se[1] < tot;
+            if ((AX & 4) && c.sz >= 0) ok = ok && c.ozc >= 0 && (int64_t)c.ozc + last * ny * t2 + 3LL * A.se[2] < tot;
+            psi_ok = psi_ok && ok;
+        }
     }
+    if (CP && !psi_ok) atomicOr(A.status, PC_STATUS_BOUNDS);  // psi traffic of this pair is skipped
+    // psi work only where this pair or the plane lies in a slab (warp-uniform for
+    // the x slabs, and mostly so for y and z with the pair order of pair_of)
+    const bool yzs = CP && psi_ok &&
+                     (((AX & 2) && rw.sy >= 0 && (pc[0].kjd || pc[1].kjd)) || ((AX & 4) && (pc[0].sz >= 0 || pc[1].sz >= 0)));
+    auto use_psi = [&](const TsPlane& P) { return CP && psi_ok && (yzs || P.sx >= 0); };
 
     float* const H1b0 = buf;
     float* const H1b1 = buf + 3 * BQ;
     float chk = 0.f;  // running sum of the stored E: non-finite iff some value was
     bool timed_out = false;
     int n = 0;
+    const float2 z2 = make_float2(0.f, 0.f);
     // carried own values of earlier planes
-    float ce0x = 0.f, ce0y = 0.f, ce0z = 0.f;  // E0(p-1)
-    float ch1x = 0.f, ch1y = 0.f, ch1z = 0.f;  // H1(p-1)
-    float cb1x = 0.f, cb1y = 0.f, cb1z = 0.f;  // Cb(p-1)
+    V3 ce0{z2, z2, z2};  // E0(p-1)
+    V3 ch1{z2, z2, z2};  // H1(p-1)
+    V3 cb1{z2, z2, z2};  // Cb(p-1)
     // psi_in of H at plane p and of E at plane p-1, loaded one plane ahead
-    P6 pfH = psi_load<AX, true>(A, pt, t2, pl0, x_slab<AX>(A, t, pl0));
-    P6 pfE = psi_load<AX, false>(A, pt, t2, pl0 - 1, x_slab<AX>(A, t, pl0 - 1));
+    P6 pfH[2], pfE[2];
+    TsPlane Pn = plane_of<AX>(A, sC, t, pl0);  // plane p of the next iteration
+    TsPlane Pq = plane_of<AX>(A, sC, t, pl0 - 1);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        pfH[h] = pfE[h] = P6{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (use_psi(Pn)) pfH[h] = psi_load<AX, true>(A, pc[h], rw.sy, psi_ok, t2, pl0, Pn.sx);
+        if (use_psi(Pq)) pfE[h] = psi_load<AX, false>(A, pc[h], rw.sy, psi_ok, t2, pl0 - 1, Pq.sx);
+    }
+    bool uu[6];
 
     if constexpr (K == 1) {
         for (; n < L; ++n) {
@@ -441,54 +584,58 @@ __device__ __forceinline__ void ts3_item(const TsArgs& A, const TsMaps& maps, co
             const int s = n % TS_S;
             const bool ok = mbar_wait_bounded(&bars[s], (uint32_t)((n / TS_S) & 1), kTsWaitLimit);
             const float* st = reinterpret_cast<const float*>(stages + s * G::STAGE);
-            const int si = pt.si;
-            const float e0x = st[si], e0y = st[BQ + si], e0z = st[2 * BQ + si];
-            float h1x = st[3 * BQ + si], h1y = st[4 * BQ + si], h1z = st[5 * BQ + si];
-            const float cbx = st[6 * BQ + si], cby = st[7 * BQ + si], cbz = st[8 * BQ + si];
-            const int sxp = x_slab<AX>(A, t, p), sxq = x_slab<AX>(A, t, q);
-            float xbp, xap, xkp, xbq, xaq, xkq;
-            x_coef(sC, t2, sxp, xbp, xap, xkp);
-            x_coef(sC, t2, sxq, xbq, xaq, xkq);
-            P6 psA = pfH, psB = pfE;
-            bool ux, uy, uz;
+            const V3 e0 = ld3(st, BQ, si);
+            V3 h1 = ld3(st + 3 * BQ, BQ, si);
+            const V3 cb = ld3(st + 6 * BQ, BQ, si);
+            const TsPlane Pp = Pn;  // plane p
+            const bool psp = use_psi(Pp), psq = use_psi(Pq);
             // A: H1(p)
-            h_upd<AX, MASK>(A, pt, st, BQ, e0x, e0y, e0z, ce0y, ce0z, p, sxp, xbp, xap, xkp, h1x, h1y, h1z, psA, ux,
-                            uy, uz);
+            h_pair<AX, MASK>(A, pc, rw, st, BQ, si, e0, ce0, Pp, psp, h1, pfH, uu);
             float* Hw = (n & 1) ? H1b1 : H1b0;
-            if (pt.act) {
-                Hw[si] = h1x;
-                Hw[BQ + si] = h1y;
-                Hw[2 * BQ + si] = h1z;
-            }
-            if (pt.own && p >= ib && p < ie) {
-                const int64_t o = (int64_t)p * PR + pt.ojk;
-                A.Hout[0][o] = h1x;
-                A.Hout[1][o] = h1y;
-                A.Hout[2][o] = h1z;
-                if (CP) psi_store<AX, true>(A, pt, t2, p, sxp, psA, ux, uy, uz);
+            if (act) st3(Hw, BQ, si, h1);
+            if (own && p >= ib && p < ie) {
+                const int64_t o = (int64_t)p * PR + ojk;
+                st2(A.Hout[0] + o, h1.x.x, h1.x.y);
+                st2(A.Hout[1] + o, h1.y.x, h1.y.y);
+                st2(A.Hout[2] + o, h1.z.x, h1.z.y);
+                if (psp) {
+                    psi_store<AX, true>(A, pc[0], rw.sy, t2, p, Pp.sx, pfH[0], uu[0], uu[1], uu[2]);
+                    psi_store<AX, true>(A, pc[1], rw.sy, t2, p, Pp.sx, pfH[1], uu[3], uu[4], uu[5]);
+                }
             }
             // B: E1(p-1)
             const float* Hr = (n & 1) ? H1b0 : H1b1;
-            float e1x = ce0x, e1y = ce0y, e1z = ce0z;
-            e_upd<AX, MASK>(A, pt, Hr, BQ, ch1x, ch1y, ch1z, h1y, h1z, q, sxq, xbq, xaq, xkq, cb1x, cb1y, cb1z, e1x,
-                            e1y, e1z, psB, ux, uy, uz);
-            if (src_item) add_src(A, pt, q, A.row0, e1x, e1y, e1z);
-            if (pt.own && q >= ib && q < ie) {
-                const int64_t o = (int64_t)q * PR + pt.ojk;
-                A.Eout[0][o] = e1x;
-                A.Eout[1][o] = e1y;
-                A.Eout[2][o] = e1z;
-                chk += (e1x + e1y) + e1z;
-                if (CP) psi_store<AX, false>(A, pt, t2, q, sxq, psB, ux, uy, uz);
+            V3 e1 = ce0;
+            e_pair<AX, MASK>(A, pc, rw, Hr, BQ, si, ch1, h1, cb1, Pq, psq, e1, pfE, uu);
+            if (src_item) {
+                add_src(A, j, kp, q, A.row0, e1.x.x, e1.y.x, e1.z.x);
+                add_src(A, j, kp + 1, q, A.row0, e1.x.y, e1.y.y, e1.z.y);
             }
-            // next plane's psi, then the carries
+            if (own && q >= ib && q < ie) {
+                const int64_t o = (int64_t)q * PR + ojk;
+                st2(A.Eout[0] + o, e1.x.x, e1.x.y);
+                st2(A.Eout[1] + o, e1.y.x, e1.y.y);
+                st2(A.Eout[2] + o, e1.z.x, e1.z.y);
+                chk += ((e1.x.x + e1.y.x) + e1.z.x) + ((e1.x.y + e1.y.y) + e1.z.y);
+                if (psq) {
+                    psi_store<AX, false>(A, pc[0], rw.sy, t2, q, Pq.sx, pfE[0], uu[0], uu[1], uu[2]);
+                    psi_store<AX, false>(A, pc[1], rw.sy, t2, q, Pq.sx, pfE[1], uu[3], uu[4], uu[5]);
+                }
+            }
+            // next plane's state and psi, then the carries
+            Pn = plane_of<AX>(A, sC, t, p + 1);
+            Pq = Pp;
             if (CP) {
-                pfH = psi_load<AX, true>(A, pt, t2, p + 1, x_slab<AX>(A, t, p + 1));
-                pfE = psi_load<AX, false>(A, pt, t2, p, sxp);
+                const bool psn = use_psi(Pn);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (psn) pfH[h] = psi_load<AX, true>(A, pc[h], rw.sy, psi_ok, t2, p + 1, Pn.sx);
+                    if (psp) pfE[h] = psi_load<AX, false>(A, pc[h], rw.sy, psi_ok, t2, p, Pp.sx);
+                }
             }
-            ce0x = e0x, ce0y = e0y, ce0z = e0z;
-            ch1x = h1x, ch1y = h1y, ch1z = h1z;
-            cb1x = cbx, cb1y = cby, cb1z = cbz;
+            ce0 = e0;
+            ch1 = h1;
+            cb1 = cb;
             if (__syncthreads_or(!ok)) {
                 timed_out = true;
                 break;
@@ -503,48 +650,37 @@ __device__ __forceinline__ void ts3_item(const TsArgs& A, const TsMaps& maps, co
         float* const E1b1 = buf + 9 * BQ;
         float* const H2b0 = buf + 12 * BQ;
         float* const H2b1 = buf + 15 * BQ;
-        float ce1x = 0.f, ce1y = 0.f, ce1z = 0.f;  // E1(p-2)
-        float ch2x = 0.f, ch2y = 0.f, ch2z = 0.f;  // H2(p-2)
-        float cb2x = 0.f, cb2y = 0.f, cb2z = 0.f;  // Cb(p-2)
-        P6 cpH{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};     // psi after step 1: H at p-1
-        P6 cpE{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};     // psi after step 1: E at p-2
+        V3 ce1{z2, z2, z2};  // E1(p-2)
+        V3 ch2{z2, z2, z2};  // H2(p-2)
+        V3 cb2{z2, z2, z2};  // Cb(p-2)
+        P6 cpH[2], cpE[2];   // psi after step 1: H at p-1, E at p-2
+#pragma unroll
+        for (int h = 0; h < 2; ++h) cpH[h] = cpE[h] = P6{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        TsPlane Pq2 = plane_of<AX>(A, sC, t, pl0 - 2);
         for (; n < L; ++n) {
             const int p = pl0 + n, q = p - 1, q2 = p - 2;
             const int s = n % TS_S;
             const bool ok = mbar_wait_bounded(&bars[s], (uint32_t)((n / TS_S) & 1), kTsWaitLimit);
             const float* st = reinterpret_cast<const float*>(stages + s * G::STAGE);
-            const int si = pt.si;
-            const float e0x = st[si], e0y = st[BQ + si], e0z = st[2 * BQ + si];
-            float h1x = st[3 * BQ + si], h1y = st[4 * BQ + si], h1z = st[5 * BQ + si];
-            const float cbx = st[6 * BQ + si], cby = st[7 * BQ + si], cbz = st[8 * BQ + si];
-            const int sxp = x_slab<AX>(A, t, p), sxq = x_slab<AX>(A, t, q), sxq2 = x_slab<AX>(A, t, q2);
-            float xbp, xap, xkp, xbq, xaq, xkq, xbq2, xaq2, xkq2;
-            x_coef(sC, t2, sxp, xbp, xap, xkp);
-            x_coef(sC, t2, sxq, xbq, xaq, xkq);
-            x_coef(sC, t2, sxq2, xbq2, xaq2, xkq2);
-            P6 psA = pfH, psB = pfE;
-            bool ux, uy, uz;
+            const V3 e0 = ld3(st, BQ, si);
+            V3 h1 = ld3(st + 3 * BQ, BQ, si);
+            const V3 cb = ld3(st + 6 * BQ, BQ, si);
+            const TsPlane Pp = Pn;  // plane p (Pq: p-1, Pq2: p-2)
+            const bool psp = use_psi(Pp), psq = use_psi(Pq), psq2 = use_psi(Pq2);
             // A: H1(p)
-            h_upd<AX, MASK>(A, pt, st, BQ, e0x, e0y, e0z, ce0y, ce0z, p, sxp, xbp, xap, xkp, h1x, h1y, h1z, psA, ux,
-                            uy, uz);
+            h_pair<AX, MASK>(A, pc, rw, st, BQ, si, e0, ce0, Pp, psp, h1, pfH, uu);
             float* H1w = (n & 1) ? H1b1 : H1b0;
-            if (pt.act) {
-                H1w[si] = h1x;
-                H1w[BQ + si] = h1y;
-                H1w[2 * BQ + si] = h1z;
-            }
+            if (act) st3(H1w, BQ, si, h1);
             // B: E1(p-1)
             const float* H1r = (n & 1) ? H1b0 : H1b1;
-            float e1x = ce0x, e1y = ce0y, e1z = ce0z;
-            e_upd<AX, MASK>(A, pt, H1r, BQ, ch1x, ch1y, ch1z, h1y, h1z, q, sxq, xbq, xaq, xkq, cb1x, cb1y, cb1z, e1x,
-                            e1y, e1z, psB, ux, uy, uz);
-            if (src_item) add_src(A, pt, q, A.row0, e1x, e1y, e1z);
-            float* E1w = (n & 1) ? E1b0 : E1b1;
-            if (pt.act) {
-                E1w[si] = e1x;
-                E1w[BQ + si] = e1y;
-                E1w[2 * BQ + si] = e1z;
+            V3 e1 = ce0;
+            e_pair<AX, MASK>(A, pc, rw, H1r, BQ, si, ch1, h1, cb1, Pq, psq, e1, pfE, uu);
+            if (src_item) {
+                add_src(A, j, kp, q, A.row0, e1.x.x, e1.y.x, e1.z.x);
+                add_src(A, j, kp + 1, q, A.row0, e1.x.y, e1.y.y, e1.z.y);
             }
+            float* E1w = (n & 1) ? E1b0 : E1b1;
+            if (act) st3(E1w, BQ, si, e1);
             if (__syncthreads_or(!ok)) {
                 timed_out = true;
                 break;
@@ -553,52 +689,60 @@ __device__ __forceinline__ void ts3_item(const TsArgs& A, const TsMaps& maps, co
                 issue(n + TS_S);
                 ++issued;
             }
-            // C: H2(p-1) from E1(p-1) (E1w) and this point's E1(p-2)
-            float h2x = ch1x, h2y = ch1y, h2z = ch1z;
-            P6 psC = cpH;
-            h_upd<AX, MASK>(A, pt, E1w, BQ, e1x, e1y, e1z, ce1y, ce1z, q, sxq, xbq, xaq, xkq, h2x, h2y, h2z, psC, ux,
-                            uy, uz);
+            // C: H2(p-1) from E1(p-1) (E1w) and this pair's E1(p-2)
+            V3 h2 = ch1;
+            h_pair<AX, MASK>(A, pc, rw, E1w, BQ, si, e1, ce1, Pq, psq, h2, cpH, uu);
             float* H2w = (n & 1) ? H2b0 : H2b1;
-            if (pt.act) {
-                H2w[si] = h2x;
-                H2w[BQ + si] = h2y;
-                H2w[2 * BQ + si] = h2z;
-            }
-            if (pt.own && q >= ib && q < ie) {
-                const int64_t o = (int64_t)q * PR + pt.ojk;
-                A.Hout[0][o] = h2x;
-                A.Hout[1][o] = h2y;
-                A.Hout[2][o] = h2z;
-                if (CP) psi_store<AX, true>(A, pt, t2, q, sxq, psC, ux, uy, uz);
+            if (act) st3(H2w, BQ, si, h2);
+            if (own && q >= ib && q < ie) {
+                const int64_t o = (int64_t)q * PR + ojk;
+                st2(A.Hout[0] + o, h2.x.x, h2.x.y);
+                st2(A.Hout[1] + o, h2.y.x, h2.y.y);
+                st2(A.Hout[2] + o, h2.z.x, h2.z.y);
+                if (psq) {
+                    psi_store<AX, true>(A, pc[0], rw.sy, t2, q, Pq.sx, cpH[0], uu[0], uu[1], uu[2]);
+                    psi_store<AX, true>(A, pc[1], rw.sy, t2, q, Pq.sx, cpH[1], uu[3], uu[4], uu[5]);
+                }
             }
             // D: E2(p-2) from H2(p-2) (written in the previous iteration) and H2(p-1)
             const float* H2r = (n & 1) ? H2b1 : H2b0;
-            float e2x = ce1x, e2y = ce1y, e2z = ce1z;
-            P6 psD = cpE;
-            e_upd<AX, MASK>(A, pt, H2r, BQ, ch2x, ch2y, ch2z, h2y, h2z, q2, sxq2, xbq2, xaq2, xkq2, cb2x, cb2y, cb2z,
-                            e2x, e2y, e2z, psD, ux, uy, uz);
-            if (src_item) add_src(A, pt, q2, A.row0 + 1, e2x, e2y, e2z);
-            if (pt.own && q2 >= ib && q2 < ie) {
-                const int64_t o = (int64_t)q2 * PR + pt.ojk;
-                A.Eout[0][o] = e2x;
-                A.Eout[1][o] = e2y;
-                A.Eout[2][o] = e2z;
-                chk += (e2x + e2y) + e2z;
-                if (CP) psi_store<AX, false>(A, pt, t2, q2, sxq2, psD, ux, uy, uz);
+            V3 e2 = ce1;
+            e_pair<AX, MASK>(A, pc, rw, H2r, BQ, si, ch2, h2, cb2, Pq2, psq2, e2, cpE, uu);
+            if (src_item) {
+                add_src(A, j, kp, q2, A.row0 + 1, e2.x.x, e2.y.x, e2.z.x);
+                add_src(A, j, kp + 1, q2, A.row0 + 1, e2.x.y, e2.y.y, e2.z.y);
             }
-            // next plane's psi, then the carries
+            if (own && q2 >= ib && q2 < ie) {
+                const int64_t o = (int64_t)q2 * PR + ojk;
+                st2(A.Eout[0] + o, e2.x.x, e2.x.y);
+                st2(A.Eout[1] + o, e2.y.x, e2.y.y);
+                st2(A.Eout[2] + o, e2.z.x, e2.z.y);
+                chk += ((e2.x.x + e2.y.x) + e2.z.x) + ((e2.x.y + e2.y.y) + e2.z.y);
+                if (psq2) {
+                    psi_store<AX, false>(A, pc[0], rw.sy, t2, q2, Pq2.sx, cpE[0], uu[0], uu[1], uu[2]);
+                    psi_store<AX, false>(A, pc[1], rw.sy, t2, q2, Pq2.sx, cpE[1], uu[3], uu[4], uu[5]);
+                }
+            }
+            // next plane's state and psi, then the carries
+            Pq2 = Pq;
+            Pq = Pp;
+            Pn = plane_of<AX>(A, sC, t, p + 1);
             if (CP) {
-                pfH = psi_load<AX, true>(A, pt, t2, p + 1, x_slab<AX>(A, t, p + 1));
-                pfE = psi_load<AX, false>(A, pt, t2, p, sxp);
-                cpH = psA;
-                cpE = psB;
+                const bool psn = use_psi(Pn);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (psp) cpH[h] = pfH[h];  // H psi of plane p after step 1
+                    if (psq) cpE[h] = pfE[h];  // E psi of plane p-1 after step 1
+                    if (psn) pfH[h] = psi_load<AX, true>(A, pc[h], rw.sy, psi_ok, t2, p + 1, Pn.sx);
+                    if (psp) pfE[h] = psi_load<AX, false>(A, pc[h], rw.sy, psi_ok, t2, p, Pp.sx);
+                }
             }
-            ce0x = e0x, ce0y = e0y, ce0z = e0z;
-            ch1x = h1x, ch1y = h1y, ch1z = h1z;
-            ce1x = e1x, ce1y = e1y, ce1z = e1z;
-            ch2x = h2x, ch2y = h2y, ch2z = h2z;
-            cb2x = cb1x, cb2y = cb1y, cb2z = cb1z;
-            cb1x = cbx, cb1y = cby, cb1z = cbz;
+            ce0 = e0;
+            ch1 = h1;
+            ce1 = e1;
+            ch2 = h2;
+            cb2 = cb1;
+            cb1 = cb;
         }
     }
     if (!isfinite(chk)) atomicOr(A.status, PC_STATUS_NONFINITE);
@@ -636,7 +780,7 @@ struct TsState {
     bool ready = false;
     int4* d_items[2] = {nullptr, nullptr};
     int nitems[2] = {0, 0}, items_cap[2] = {0, 0};
-    int64_t items_key[2][3] = {{-1, -1, -1}, {-1, -1, -1}};  // chunk, t, source generation
+    int64_t items_key[2][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}};  // chunk, t, source generation, order
     TsSrc* d_src = nullptr;  // TS_MAX_SRC entries
     int nsrc = 0;
     int64_t src_gen = -1;
@@ -707,7 +851,8 @@ template <int K>
 int ts_items(pc_ctx* c, TsState* st, int cx, cudaStream_t stream) {
     const int ki = K - 1;
     const int t = c->cpml_t;
-    if (st->items_key[ki][0] == cx && st->items_key[ki][1] == t && st->items_key[ki][2] == st->src_gen)
+    if (st->items_key[ki][0] == cx && st->items_key[ki][1] == t && st->items_key[ki][2] == st->src_gen &&
+        st->items_key[ki][3] == c->ts_order)
         return PC_OK;
     const pc_grid_desc& g = c->g;
     auto touches_slab = [&](int lo, int hi, int n) {  // [lo, hi) against the slabs of an axis of length n
@@ -716,7 +861,10 @@ int ts_items(pc_ctx* c, TsState* st, int cx, cudaStream_t stream) {
         return a < b && (a < t || b > n - t);
     };
     auto outside_interior = [&](int lo, int hi, int n) { return lo < 1 || hi > n - 1; };
+    static const float kCost[TC_N] = {1.0f, 1.2f, 1.8f, 1.8f, 1.8f, 2.5f};  // relative time per plane
     std::vector<int4> h;
+    std::vector<float> cost;
+    std::vector<int> chunk;
     for (int ib = 0; ib < g.nx; ib += cx)
         for (int j0 = 0; j0 < g.ny; j0 += TS_TY)
             for (int k0 = 0; k0 < g.nz; k0 += TS_TZ) {
@@ -740,7 +888,31 @@ int ts_items(pc_ctx* c, TsState* st, int cx, cudaStream_t stream) {
                     src = src || (s.i >= plo && s.i < phi && s.j >= jlo && s.j < jhi && s.k >= klo && s.k < khi);
                 const int w = ie | (cls << 20) | ((src && st->src_ok) ? (1 << 28) : 0);
                 h.push_back(make_int4(k0, j0, ib, w));
+                cost.push_back(kCost[cls] * (float)(ie - ib + 2 * K));
+                chunk.push_back(ib / cx);
             }
+    if (c->ts_order != 0) {
+        // order 1: x-chunks by their summed cost, most expensive first (the slab
+        // chunks), and within a chunk the slower items first; the tiles of one
+        // chunk still run together (one chunk is about one wave of CTAs), so their
+        // shared halo rows are read from L2.  order 2: every item by cost.
+        const int nch = (g.nx + cx - 1) / cx;
+        std::vector<float> csum(nch, 0.f);
+        for (size_t q = 0; q < h.size(); ++q) csum[chunk[q]] += cost[q];
+        std::vector<int> ord(h.size());
+        for (size_t q = 0; q < ord.size(); ++q) ord[q] = (int)q;
+        const bool by_item = c->ts_order == 2;
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+            if (!by_item && chunk[a] != chunk[b]) {
+                if (csum[chunk[a]] != csum[chunk[b]]) return csum[chunk[a]] > csum[chunk[b]];
+                return chunk[a] < chunk[b];
+            }
+            return cost[a] > cost[b];
+        });
+        std::vector<int4> o(h.size());
+        for (size_t q = 0; q < ord.size(); ++q) o[q] = h[ord[q]];
+        h.swap(o);
+    }
     if ((int)h.size() > st->items_cap[ki]) {
         cudaFree(st->d_items[ki]);  // synchronises the device: no launch still reads it
         st->d_items[ki] = nullptr;
@@ -756,6 +928,7 @@ int ts_items(pc_ctx* c, TsState* st, int cx, cudaStream_t stream) {
     st->items_key[ki][0] = cx;
     st->items_key[ki][1] = t;
     st->items_key[ki][2] = st->src_gen;
+    st->items_key[ki][3] = c->ts_order;
     return PC_OK;
 }
 

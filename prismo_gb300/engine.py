@@ -433,34 +433,44 @@ class FDTDEngine:
         _lib.check(self.lib.pc_profile_read(self.ctx, C.byref(ms), C.byref(n)), "pc_profile_read")
         return float(ms.value), int(n.value), steps
 
-    def set_time_blocking(self, steps: int, chunk: int = 0):
+    def set_time_blocking(self, steps: int, chunk: int = 0, order: Optional[int] = None):
         """Time steps per launch of the temporally blocked 3D stepper (2: two steps
         per launch wherever no monitor samples the step in between, 1: one, 0:
-        off, the fused schedule runs) and its x-chunk length (0: automatic)."""
+        off, the fused schedule runs), its x-chunk length (0: automatic) and its
+        work-item order (0 grid order, 1 expensive chunks first, 2 by item cost)."""
         _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_TS_STEPS, int(steps)), "pc_set_tuning")
         _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_TS_CHUNK, int(chunk)), "pc_set_tuning")
+        if order is not None:
+            _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_TS_ORDER, int(order)), "pc_set_tuning")
 
     def time_blocking(self):
         return (int(self.lib.pc_get_tuning(self.ctx, _lib.PC_TUNE_TS_STEPS)),
-                int(self.lib.pc_get_tuning(self.ctx, _lib.PC_TUNE_TS_CHUNK)))
+                int(self.lib.pc_get_tuning(self.ctx, _lib.PC_TUNE_TS_CHUNK)),
+                int(self.lib.pc_get_tuning(self.ctx, _lib.PC_TUNE_TS_ORDER)))
+
+    def time_blocking_active(self) -> bool:
+        """Whether the temporally blocked stepper runs for this configuration."""
+        return bool(self.lib.pc_get_tuning(self.ctx, _lib.PC_TUNE_TS_ACTIVE))
 
     # -- autotuning ---------------------------------------------------------------
     def autotune(self, candidates=(8, 16, 24, 32, 48, 64, 96), steps: int = 20, cache: bool = True):
-        """Pick the x-chunk lengths of the fused 3D schedule by timing a few steps of
-        each candidate with CUDA events: first one length for every tile, then,
-        with that fixed for the inner tiles, the length for tiles that touch a y or
-        z CPML slab.  The fields and psi are restored afterwards.  Returns
-        (chunk, edge chunk).  Results are cached per (dims, CPML thickness,
-        precision) in ``$PRISMO_GB300_CACHE`` (default
-        ~/.cache/prismo_gb300/tune.json)."""
+        """Pick the x-chunk lengths of the 3D schedule by timing a few steps of each
+        candidate with CUDA events.  Fused schedule: first one length for every
+        tile, then, with that fixed for the inner tiles, the length for tiles that
+        touch a y or z CPML slab; returns (chunk, edge chunk).  Temporally blocked
+        stepper: the chunk length, then the work-item order; returns (chunk,
+        order).  The fields and psi are restored afterwards.  Results are cached
+        per (dims, CPML thickness, precision, schedule) in ``$PRISMO_GB300_CACHE``
+        (default ~/.cache/prismo_gb300/tune.json)."""
         import json
         import os
 
         torch = _torch()
         if self.is_2d or not self.pingpong:
             return None
+        blocked = self.time_blocking_active()
         key = f"{self.dims}|t={0 if self.pml is None else self.pml.thickness}|{self.precision}|" \
-              f"{torch.cuda.get_device_name(self.device)}"
+              f"{'ts' if blocked else 'fused'}|{torch.cuda.get_device_name(self.device)}"
         path = os.environ.get("PRISMO_GB300_CACHE", os.path.join(os.path.expanduser("~"), ".cache",
                                                                  "prismo_gb300", "tune.json"))
         table = {}
@@ -472,7 +482,10 @@ class FDTDEngine:
                 table = {}
         if cache and isinstance(table.get(key), list) and len(table[key]) == 2:
             cx, ce = (int(v) for v in table[key])
-            self.set_chunk(cx, ce)
+            if blocked:
+                self.set_time_blocking(self.time_blocking()[0], cx, ce)
+            else:
+                self.set_chunk(cx, ce)
             return cx, ce
         saved_sets = [t.clone() for t in self.sets]
         saved_psi = [t.clone() for t in self.psi]
@@ -480,8 +493,13 @@ class FDTDEngine:
         nsrc = len(self.sources)
         amps = np.zeros((steps, nsrc)) if nsrc else None
 
+        ts_steps = self.time_blocking()[0]
+
         def timed(cx, ce):
-            self.set_chunk(cx, ce)
+            if blocked:  # (chunk, work-item order) of the temporally blocked stepper
+                self.set_time_blocking(ts_steps, cx, ce)
+            else:
+                self.set_chunk(cx, ce)
             self.step(2, None if amps is None else amps[:2])
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
@@ -494,11 +512,17 @@ class FDTDEngine:
         cands = [c for c in candidates if c < self.dims[0]]
         best, best_ms = None, float("inf")
         for cx in cands:
-            ms = timed(cx, 0)
+            ms = timed(cx, 2 if blocked else 0)
             if ms < best_ms:
                 best, best_ms = cx, ms
-        best_e = 0
-        if best is not None and self.pml is not None:
+        best_e = 2 if blocked else 0
+        if blocked:
+            for order in (0, 1):
+                if best is not None:
+                    ms = timed(best, order)
+                    if ms < best_ms:
+                        best_e, best_ms = order, ms
+        elif best is not None and self.pml is not None:
             for ce in cands:
                 if ce == best:
                     continue
@@ -513,7 +537,10 @@ class FDTDEngine:
         self.check_status()
         if best is None:
             return None
-        self.set_chunk(best, best_e)
+        if blocked:
+            self.set_time_blocking(ts_steps, best, best_e)
+        else:
+            self.set_chunk(best, best_e)
         if cache:
             table[key] = [best, best_e]
             try:
