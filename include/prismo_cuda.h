@@ -129,10 +129,13 @@ int pc_step(pc_ctx* ctx, int32_t nsteps, const double* amps, void* stream);
  * update instead of Ca/Cb (materials/ade.py:100-160 recursions with the
  * coefficients of materials/dispersion.py:189-336, coupled to E through the
  * polarisation current):
- *   Lorentz (kind 0): P+ = C0 E+ + C1 E + C2 P + C3 P-       (aux: P, P-)
+ *   Lorentz (kind 0): P+ = C0 E+ + C1 E + C2 P + C3 P-       (aux: P, D = P - P-)
  *   Drude   (kind 1): J+ = C1 J + C0 (E+ + E)/2               (aux: J)
  *   Debye   (kind 2): P+ = C1 P + C0 (E+ + E)/2               (aux: P)
  * with eps_inf (E+ - E) + sum dP (or dt J terms) = (dt/eps0) curl H, solved for E+.
+ * The Lorentz recursion is carried as P and its last increment D: the same
+ * algebra, D+ = C0 E+ + C1 E + (C2 + C3 - 1) P - C3 D and P+ = P + D+, without
+ * the float32 cancellation of C2 P + C3 P- (C2 is close to 2 and C3 to -1).
  * aux[c][p][0..1]: caller-owned zeroed device arrays over the box (C order,
  * float context precision), per E component c and pole p. */
 typedef struct pc_ade_region {

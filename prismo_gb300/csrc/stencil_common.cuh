@@ -88,7 +88,8 @@ static AdeArgs<T> make_ade_args(pc_ctx* c) {
             A.kind[r][p] = R.kind[p];
             A.c0[r][p] = T(R.c0[p]);
             A.c1[r][p] = T(R.c1[p]);
-            A.c2[r][p] = T(R.c2[p]);
+            // Lorentz: c2 carries C2 + C3 - 1 (formed in float64) for the increment form
+            A.c2[r][p] = T(R.kind[p] == 0 ? (R.c2[p] + R.c3[p]) - 1.0 : R.c2[p]);
             A.c3[r][p] = T(R.c3[p]);
             for (int comp = 0; comp < 3; ++comp)
                 for (int w = 0; w < 2; ++w) A.aux[r][comp][p][w] = static_cast<T*>(R.aux[comp][p][w]);
@@ -110,8 +111,9 @@ __device__ __forceinline__ bool ade_update(const AdeArgs<T>& A, int comp, int i,
         for (int p = 0; p < A.npoles[r]; ++p) {
             const T a0 = A.aux[r][comp][p][0][o];
             if (A.kind[r][p] == 0) {
-                const T a1 = A.aux[r][comp][p][1][o];
-                acc -= A.inv[r] * ((A.c2[r][p] - T(1)) * a0 + A.c3[r][p] * a1);
+                // (C2 - 1) P + C3 P- = (C2 + C3 - 1) P - C3 D, with D = P - P-
+                const T d1 = A.aux[r][comp][p][1][o];
+                acc -= A.inv[r] * (A.c2[r][p] * a0 - A.c3[r][p] * d1);
             } else if (A.kind[r][p] == 1) {
                 acc -= A.inv[r] * (T(0.5) * A.dt * (T(1) + A.c1[r][p]) * a0);
             } else {
@@ -123,10 +125,11 @@ __device__ __forceinline__ bool ade_update(const AdeArgs<T>& A, int comp, int i,
             T* x0 = A.aux[r][comp][p][0];
             const T a0 = x0[o];
             if (A.kind[r][p] == 0) {
+                // D+ = C0 E+ + C1 E + (C2 + C3 - 1) P - C3 D,  P+ = P + D+
                 T* x1 = A.aux[r][comp][p][1];
-                const T pn = A.c0[r][p] * e1 + A.c1[r][p] * e0 + A.c2[r][p] * a0 + A.c3[r][p] * x1[o];
-                x1[o] = a0;
-                x0[o] = pn;
+                const T dn = (A.c0[r][p] * e1 + A.c1[r][p] * e0) + (A.c2[r][p] * a0 - A.c3[r][p] * x1[o]);
+                x1[o] = dn;
+                x0[o] = a0 + dn;
             } else {
                 x0[o] = A.c1[r][p] * a0 + A.c0[r][p] * (T(0.5) * (e1 + e0));
             }
