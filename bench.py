@@ -3,7 +3,7 @@ benchmark = one whole 2000-time-step simulation from zero fields).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--chunk CX[,EDGE]]
     python bench.py --workload 2d|dispersive|sweep|surrogate   (the other configurations)
-    python bench.py --workload mlp                             (the surrogate's forward products)
+    python bench.py --workload mlp                             (the surrogate's products, forward and training)
 
 Workload (the reference's 3D plain-FDTD configuration): 256^3 total cells at
 dx = 20 nm with a 12-cell CPML on all six faces, Courant 0.5, 32 seeded
@@ -708,6 +708,11 @@ def run_surrogate(args, cpu):
     t_data = time.perf_counter() - t0
     E = Su.Ensemble()
     E.fit(train, Str, epochs=Su.EPOCHS)
+    # gate calibration on designs held out from training and from the test set
+    calib = [S.coupler_design(s) for s in Su.CALIB_SEEDS]
+    t0 = time.perf_counter()
+    E.calibrate(calib, np.concatenate([S.batched_sweep(calib[q:q + 512]).S for q in range(0, len(calib), 512)]))
+    t_calib = time.perf_counter() - t0
     res = Su.run_pipeline(E, test)
     err = Su.s_error(res.S, ref.S)
     acc = res.accepted
@@ -747,7 +752,8 @@ def run_surrogate(args, cpu):
           config={"workload": "surrogate + batched-FDTD fallback on 256 held-out couplers (seeds 10000-10255); "
                               "4-member ensemble 31-256-256-256-512 SiLU (3 geometry floats + per-member random "
                               "Fourier embedding) trained on 4096 batched-FDTD designs (seeds 0-4095)",
-                  "threshold": Su.THRESHOLD, "epochs": Su.EPOCHS, "train_seconds": E.train_seconds,
+                  "error_bar": Su.THRESHOLD, "gate": E.calibration, "calibration_seconds": t_calib,
+                  "epochs": Su.EPOCHS, "train_seconds": E.train_seconds,
                   "train_steps": E.train_steps, "data_seconds": t_data},
           accepted=int(acc.sum()), accepted_fraction=frac,
           err_rms_answered={"median": float(np.median(err[acc])) if acc.any() else None,
@@ -758,7 +764,7 @@ def run_surrogate(args, cpu):
           batched_fdtd_designs_per_s=r_fdtd, serial_designs_per_s=ser.designs_per_s,
           pipeline_vs_serial=res.designs_per_s / ser.designs_per_s,
           inference={"queries": 8192, "seconds": t_inf, "designs_per_s": 8192 / t_inf,
-                     "accept_fraction": float(np.mean(spread_q <= Su.THRESHOLD)),
+                     "accept_fraction": float(np.mean(E.gate(q, spread_q))),
                      "device_forward_ms": fwd_ms, "device_tflops": flops / (fwd_ms * 1e-3) / 1e12,
                      "device_forward_ms_mma_sync": fwd_ms_mma,
                      "pipeline_designs_per_s_8192": dps_8192,
@@ -804,13 +810,39 @@ def run_mlp(args):
     E.set_tensor_path(False)
     y_mma = E.forward_raw(x)
     rel = float((y_tc - y_mma).norm() / y_mma.norm().clamp_min(1e-30))
+
+    # training steps (forward, loss gradient, backward products, Adam): the
+    # surrogate's 256-design batches, and 4096-design batches where the backward
+    # products fill the GPU
+    def timed_train(tc, Bt, reps=30):
+        xt = x[:, :Bt].contiguous()
+        tt = torch.zeros((E.members, Bt, dims[-1]), dtype=torch.float32, device="cuda")
+        E.set_tensor_path(tc)
+        for _ in range(5):
+            E.train_step_raw(xt, tt, 1e-6)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(reps):
+            E.train_step_raw(xt, tt, 1e-6)
+        ev1.record()
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / reps
+
+    train = {}
+    for Bt in (256, 4096):
+        fl = 3 * E.members * Bt * 2 * (32 * dims[1] + dims[1] * dims[2] + dims[2] * dims[3] + dims[3] * dims[4])
+        t = {k: timed_train(v, Bt) for k, v in (("mma_sync", False), ("tcgen05", True), ("auto", "auto"))}
+        train[f"batch_{Bt}"] = {**{f"ms_{k}": v for k, v in t.items()},
+                                "tflops_tcgen05": fl / (t["tcgen05"] * 1e-3) / 1e12}
+    E.set_tensor_path("auto")
     status = E.status()
     E.close()
     _line(metric="TFLOP/s", value=flops / (ms_tc * 1e-3) / 1e12, unit="TFLOP/s", steps=args.steps,
           warmup=args.warmup, ms_per_step=ms_tc, dtype="bf16 (f32 accumulate)",
           config={"workload": "surrogate forward: 4 members x 8192 rows, 31-256-256-256-512 SiLU, bf16 hi/lo "
                               "activations", "status": status, "tcgen05_vs_mma_sync_rel": rel},
-          mma_sync_ms_per_step=ms_mma, gpu_launches=launches)
+          mma_sync_ms_per_step=ms_mma, gpu_launches=launches, train_step_per_member_batch=train)
 
 
 if __name__ == "__main__":

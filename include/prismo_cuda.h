@@ -431,9 +431,11 @@ int pc_mlp_gradients(pc_mlp* n, const float* d_x, const float* d_t, int32_t batc
 int pc_mlp_train_step(pc_mlp* n, const float* d_x, const float* d_t, int32_t batch, float lr, float beta1,
                       float beta2, float eps, float* d_loss, void* stream);
 int64_t pc_mlp_launch_count(const pc_mlp* n);
-/* Forward products on the 5th-generation tensor cores (tcgen05.mma with a tensor
- * memory accumulator; 1, the default) or on mma.sync (0).  Output widths that
- * are not multiples of 256 always use mma.sync. */
+/* Where the products run: the 5th-generation tensor cores (tcgen05.mma with a
+ * tensor-memory accumulator; 1: every product whose shape fits), mma.sync (0),
+ * or (2, the default) tcgen05 for launches of at least 64 of its 128 x 256 tiles
+ * and mma.sync below that.  Output widths that are not multiples of 256, and
+ * unaligned outputs, always use mma.sync. */
 int pc_mlp_set_tensor_path(pc_mlp* n, int32_t tcgen05);
 /* Read the status word (PC_STATUS_TIMEOUT: a bounded wait for the tensor cores
  * ran out).  Synchronises the stream. */

@@ -16,8 +16,13 @@ namespace {
 __device__ __forceinline__ void cell_e(const double* eps, const double* sig, int64_t c, double dt,
                                        double eps0, double& ca, double& cb) {
     const double er = eps ? eps[c] : 1.0;
-    const double s = sig ? sig[c] : 0.0;
     const double e = eps0 * er;
+    if (!sig) {  // sigma = 0: q = 0, so Ca = 1 / 1 and Cb = (dt / e) / 1 exactly
+        ca = 1.0;
+        cb = dt / e;
+        return;
+    }
+    const double s = sig[c];
     const double q = s * dt / (2.0 * e);
     ca = (1.0 - q) / (1.0 + q);
     cb = (dt / e) / (1.0 + q);
@@ -93,6 +98,7 @@ __global__ void build_coef3(int nx, int ny, int nz, int pitch, const double* eps
         put<T>(out.ca[2], o, 0.0);
         put<T>(out.cb[2], o, 0.0);
     }
+    if (!out.da[0] && !out.db[0] && !out.da[1] && !out.db[1] && !out.da[2] && !out.db[2]) return;
     // Hx: (i+1/2, j, k), mean over x
     if (i < nx - 1 && k < nz) {
         cell_h(mu, sigm, cid(i, j, k), dt, mu0, a0, b0);

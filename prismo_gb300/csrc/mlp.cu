@@ -226,7 +226,7 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
 
 template <int MODE, bool SPLIT>
 __global__ void __launch_bounds__(TC_THREADS) mlp_gemm_tc(GemmP p, unsigned* status) {
-    static_assert(MODE == EP_HIDDEN || MODE == EP_OUT, "forward epilogues only");
+    static_assert(!SPLIT || MODE == EP_HIDDEN || MODE == EP_OUT, "split operands in forward products only");
     constexpr int NSCR = MODE == EP_HIDDEN ? 2 : 1;  // pre-activation (+ activation) slices
     static_assert(TC_THREADS / 32 * NSCR * TC_SCR * 4 <= TC_NST * tc_stage_bytes<SPLIT>(),
                   "epilogue scratch fits the stages");
@@ -326,6 +326,45 @@ __global__ void __launch_bounds__(TC_THREADS) mlp_gemm_tc(GemmP p, unsigned* sta
             float v[32];
             tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c, v);
             const int nb = n0 + c;
+            if (MODE == EP_BWD || MODE == EP_WGRAD) {
+                // lane = row: the accumulator slice to shared memory
+#pragma unroll
+                for (int j = 0; j < 32; j += 4)
+                    *reinterpret_cast<float4*>(&sx[lane * 36 + j]) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                __syncwarp();
+                // row-major: 8 lanes per row, 4 columns each (coalesced)
+#pragma unroll
+                for (int r0 = 0; r0 < 32; r0 += 4) {
+                    const int r = r0 + rr;
+                    const int64_t m = mw + r;
+                    if (m >= p.M) continue;
+                    float4 x = *reinterpret_cast<const float4*>(&sx[r * 36 + cq]);
+                    if (MODE == EP_WGRAD) {
+                        *reinterpret_cast<float4*>(&p.outF[z * p.sO + m * p.ldo + nb + cq]) = x;
+                    } else {
+                        // g = (g W) silu'(z): bf16 in both layouts, the same values as mma.sync's epilogue
+                        const float4 zz = *reinterpret_cast<const float4*>(&p.zprev[z * p.sZ + m * p.ldz + nb + cq]);
+                        float* xp = &x.x;
+                        const float* zp = &zz.x;
+#pragma unroll
+                        for (int t = 0; t < 4; ++t) {
+                            const float sg = sigm(zp[t]);
+                            xp[t] = __bfloat162float(__float2bfloat16_rn(xp[t] * (sg * (1.0f + zp[t] * (1.0f - sg)))));
+                        }
+                        *reinterpret_cast<uint2*>(&p.outB[z * p.sOB + m * p.ldb2 + nb + cq]) =
+                            make_uint2(pack_bf16x2(x.x, x.y), pack_bf16x2(x.z, x.w));
+                        *reinterpret_cast<float4*>(&sx[r * 36 + cq]) = x;
+                    }
+                }
+                __syncwarp();
+                if (MODE == EP_BWD && rowv) {  // lane = row again: the transposed copy
+#pragma unroll
+                    for (int j = 0; j < 32; ++j)
+                        p.outT[z * p.sOT + (int64_t)(nb + j) * p.ldt + mw + lane] = __float2bfloat16_rn(sx[lane * 36 + j]);
+                }
+                __syncwarp();
+                continue;
+            }
             const float bn = bias[nb + lane];
 #pragma unroll
             for (int j = 0; j < 32; j += 4) {
@@ -509,7 +548,7 @@ struct pc_mlp {
     bf16* grT[4] = {};
     float* d_loss = nullptr;
     long long t = 0;     // Adam steps taken
-    int tc = 1;          // forward products on tcgen05 (1) or mma.sync (0)
+    int tc = 2;          // products on tcgen05 (1), mma.sync (0), or by launch size (2)
     unsigned* d_status = nullptr;
     long long launches = 0;
     std::vector<void*> allocs;
@@ -553,13 +592,23 @@ int gemm(pc_mlp* n, GemmP p, cudaStream_t s) {
     return PC_OK;
 }
 
+// tcgen05 takes a product on request (tc 1), or (tc 2) when its 128 x 256 tiles
+// give the launch at least TC_MIN_CTAS CTAs: smaller products (a 256-row training
+// batch gives 8) finish sooner as the 64 x 64 tiles of mma.sync.
+constexpr int TC_MIN_CTAS = 64;
+inline bool use_tc(const pc_mlp* n, const GemmP& p) {
+    if (n->tc == 0) return false;
+    if (n->tc == 1) return true;
+    return (int64_t)(p.N / TC_N) * ((p.M + TC_M - 1) / TC_M) * n->members >= TC_MIN_CTAS;
+}
+
 // forward products (split activations): tcgen05 when the shape fits its tiles
 template <int MODE>
 int gemm_fwd(pc_mlp* n, GemmP p, cudaStream_t s) {
     // the epilogue stores 4 columns (16 bytes of float32) at a time: the output (a
     // caller's buffer for the last layer) and its strides must keep that aligned
     const bool aligned = ((uintptr_t)p.outF & 15) == 0 && p.ldo % 4 == 0 && p.sO % 4 == 0;
-    if (!n->tc || !aligned || p.N % TC_N != 0 || p.K % TC_K != 0) return gemm<MODE, true>(n, p, s);
+    if (!use_tc(n, p) || !aligned || p.N % TC_N != 0 || p.K % TC_K != 0) return gemm<MODE, true>(n, p, s);
     // at least 110 KB of shared memory: at most two CTAs per SM, so that their 2 x 256
     // tensor-memory columns fit the SM's 512 and no allocation ever waits
     constexpr int smem = tc_smem_bytes<true>() > 110 * 1024 ? tc_smem_bytes<true>() : 110 * 1024;
@@ -570,6 +619,27 @@ int gemm_fwd(pc_mlp* n, GemmP p, cudaStream_t s) {
     }
     dim3 grd(p.N / TC_N, (p.M + TC_M - 1) / TC_M, n->members);
     mlp_gemm_tc<MODE, true><<<grd, TC_THREADS, smem, s>>>(p, n->d_status);
+    ++n->launches;
+    PC_CUDA_CHECK(cudaGetLastError());
+    return PC_OK;
+}
+
+// backward products (data gradient, weight gradient) on tcgen05 when the shape fits
+template <int MODE>
+int gemm_bwd(pc_mlp* n, GemmP p, cudaStream_t s) {
+    const bool aligned = MODE == EP_WGRAD ? (((uintptr_t)p.outF & 15) == 0 && p.ldo % 4 == 0 && p.sO % 4 == 0)
+                                          : (((uintptr_t)p.outB & 7) == 0 && p.ldb2 % 4 == 0 && p.sOB % 4 == 0 &&
+                                             ((uintptr_t)p.zprev & 15) == 0 && p.ldz % 4 == 0 && p.sZ % 4 == 0);
+    const bool operands = p.lda % 8 == 0 && p.ldb % 8 == 0 && p.sA % 8 == 0 && p.sB % 8 == 0;
+    if (!use_tc(n, p) || !aligned || !operands || p.N % TC_N != 0 || p.K % TC_K != 0) return gemm<MODE>(n, p, s);
+    constexpr int smem = tc_smem_bytes<false>() > 110 * 1024 ? tc_smem_bytes<false>() : 110 * 1024;
+    static bool attr = false;
+    if (!attr) {
+        PC_CUDA_CHECK(cudaFuncSetAttribute(mlp_gemm_tc<MODE, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr = true;
+    }
+    dim3 grd(p.N / TC_N, (p.M + TC_M - 1) / TC_M, n->members);
+    mlp_gemm_tc<MODE, false><<<grd, TC_THREADS, smem, s>>>(p, n->d_status);
     ++n->launches;
     PC_CUDA_CHECK(cudaGetLastError());
     return PC_OK;
@@ -641,7 +711,7 @@ int backward(pc_mlp* n, const float* tg, int B, float* loss, cudaStream_t s) {
         p.outF = n->g + n->seg[l].w_off;
         p.ldo = n->kp[l];
         p.sO = n->P;
-        int rc = gemm<EP_WGRAD>(n, p, s);
+        int rc = gemm_bwd<EP_WGRAD>(n, p, s);
         if (rc) return rc;
         mlp_bias_grad<<<dim3((n->nn[l] + 7) / 8, M), 256, 0, s>>>(n->grT[l], n->nn[l], B, n->max_batch,
                                                                    n->g + n->seg[l].b_off, n->P);
@@ -667,7 +737,7 @@ int backward(pc_mlp* n, const float* tg, int B, float* loss, cudaStream_t s) {
         q.outT = n->grT[l - 1];
         q.ldt = B;
         q.sOT = (int64_t)n->max_batch * n->nn[l - 1];
-        rc = gemm<EP_BWD>(n, q, s);
+        rc = gemm_bwd<EP_BWD>(n, q, s);
         if (rc) return rc;
     }
     return PC_OK;
@@ -807,7 +877,7 @@ int pc_mlp_train_step(pc_mlp* n, const float* d_x, const float* d_t, int32_t bat
 int64_t pc_mlp_launch_count(const pc_mlp* n) { return n ? n->launches : PC_ERR_INVALID; }
 
 int pc_mlp_set_tensor_path(pc_mlp* n, int32_t tcgen05) {
-    if (!n || (tcgen05 != 0 && tcgen05 != 1)) return PC_ERR_INVALID;
+    if (!n || tcgen05 < 0 || tcgen05 > 2) return PC_ERR_INVALID;
     n->tc = tcgen05;
     return PC_OK;
 }

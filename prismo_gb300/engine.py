@@ -184,7 +184,9 @@ class FDTDEngine:
         sp = self._stream_ptr()
         ptr = lambda t: None if t is None else t.data_ptr()  # noqa: E731
         _lib.check(self.lib.pc_build_coefficients(
-            self.ctx, ptr(eps), ptr(mu), ptr(sig), ptr(sigm), EPS0, MU0,
+            # all-zero sigma (or mu = 1, sigma_m = 0) arrays give the same bits as none
+            self.ctx, ptr(eps), ptr(mu) if need_h else None, ptr(sig) if need_ca else None,
+            ptr(sigm) if need_h else None, EPS0, MU0,
             _lib.ptr3(ca) if need_ca else None, _lib.ptr3(cb),
             _lib.ptr3(da) if need_h else None, _lib.ptr3(db) if need_h else None, sp),
             "pc_build_coefficients")

@@ -14,8 +14,13 @@ phase exp(-i beta L) that an MLP of three inputs could not follow; predictions
 are re-embedded with the same factors, so |S - S_fdtd| = |S' - S'_fdtd| exactly.
 
 The plain FDTD stays the fallback: a design whose ensemble spread (RMS over the
-512 outputs of the standard deviation across members) exceeds ``threshold`` is
-simulated by the batched FDTD instead.
+512 outputs of the standard deviation across members) exceeds the gate's
+threshold is simulated by the batched FDTD instead.  The threshold is calibrated
+(``Ensemble.calibrate``) on designs held out from training whose FDTD spectra are
+known: the largest spread at which a stated fraction of the admitted designs lie
+within the error bar, so that the gate bounds the predicted error rather than
+the raw spread; its thresholds are set per coupling-length band, since the
+error depends mainly on the coupling length.
 """
 
 from __future__ import annotations
@@ -35,7 +40,10 @@ MEMBERS = 4
 N_RFF = 14  # random Fourier pairs per member: 3 + 2 x 14 = 31 network inputs
 RFF_SIGMA = 2.0
 DIMS = (3 + 2 * N_RFF, 256, 256, 256, 512)
-THRESHOLD = 1e-3
+THRESHOLD = 1e-3  # S-parameter error bar (RMS over the 512 outputs)
+CALIB_QUANTILE = 0.98  # fraction of the calibration designs the gate admits that must be within it
+CALIB_SEEDS = range(5000, 6024)  # calibration designs (training: 0-4095, held-out tests: 10000+)
+CALIB_BINS = 8  # gate thresholds per coupling-length band (the error's main dependence)
 EPOCHS = 2000
 
 
@@ -204,9 +212,11 @@ class Ensemble:
     def launches(self) -> int:
         return int(self.lib.pc_mlp_launch_count(self.h))
 
-    def set_tensor_path(self, tcgen05: bool):
-        """Forward products on tcgen05 (True) or mma.sync (False)."""
-        _lib.check(self.lib.pc_mlp_set_tensor_path(self.h, 1 if tcgen05 else 0), "pc_mlp_set_tensor_path")
+    def set_tensor_path(self, tcgen05):
+        """Products on tcgen05 wherever the shape fits (True), on mma.sync (False),
+        or chosen by launch size ("auto", the default)."""
+        mode = 2 if tcgen05 == "auto" else (1 if tcgen05 else 0)
+        _lib.check(self.lib.pc_mlp_set_tensor_path(self.h, mode), "pc_mlp_set_tensor_path")
 
     def status(self) -> int:
         v = C.c_uint32(0)
@@ -302,6 +312,45 @@ class Ensemble:
         S_m = np.stack([from_real(y[m], nfreq) / ph for m in range(self.members)]) if members else None
         return S, spread, S_m
 
+    def calibrate(self, designs: Sequence[SW.CouplerDesign], S_ref: np.ndarray, target: float = THRESHOLD,
+                  quantile: float = CALIB_QUANTILE, bins: int = CALIB_BINS) -> np.ndarray:
+        """Set the gate from designs held out from training with known FDTD
+        S-parameters, one threshold per coupling-length band: admitting the band's
+        designs in order of increasing spread, the largest spread at which at least
+        ``quantile`` of the admitted designs lie within ``target`` (0 admits none).
+        Returns the per-band thresholds."""
+        S, spread, _ = self.predict(designs)
+        err = s_error(S, S_ref)
+        band = self._band(designs, bins)
+        thr = np.zeros(bins)
+        admitted = np.zeros(bins, dtype=int)
+        for b in range(bins):
+            sel = np.nonzero(band == b)[0]
+            order = sel[np.argsort(spread[sel], kind="stable")]
+            ok = err[order] <= target
+            frac = np.cumsum(ok) / np.arange(1, len(ok) + 1)
+            good = np.nonzero(frac >= quantile)[0]
+            if len(good):
+                thr[b] = spread[order][good[-1]]
+                admitted[b] = good[-1] + 1
+        self.thresholds = thr
+        self.calibration = {"designs": len(designs), "target": target, "quantile": quantile, "bands": bins,
+                            "admitted": admitted.tolist(), "thresholds": thr.tolist()}
+        return thr
+
+    @staticmethod
+    def _band(designs: Sequence[SW.CouplerDesign], bins: int) -> np.ndarray:
+        L = np.array([d.params()[2] for d in designs])
+        return np.clip((L * bins).astype(int), 0, bins - 1)
+
+    def gate(self, designs: Sequence[SW.CouplerDesign], spread: np.ndarray, threshold=None) -> np.ndarray:
+        """Which designs the ensemble answers: spread under the calibrated band
+        threshold (or under ``threshold`` / ``THRESHOLD`` without a calibration)."""
+        thr = getattr(self, "thresholds", None)
+        if threshold is not None or thr is None:
+            return spread <= (THRESHOLD if threshold is None else threshold)
+        return spread <= thr[self._band(designs, len(thr))]
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.pc_mlp_destroy(self.h)
@@ -337,15 +386,17 @@ def s_error(S_a: np.ndarray, S_b: np.ndarray) -> np.ndarray:
     return np.sqrt(np.mean(d * d, axis=1))
 
 
-def run_pipeline(model: Ensemble, designs: Sequence[SW.CouplerDesign], threshold: float = THRESHOLD,
+def run_pipeline(model: Ensemble, designs: Sequence[SW.CouplerDesign], threshold=None,
                  nsteps: int = SW.STEPS, device=None) -> PipelineResult:
-    """Surrogate answers where the ensemble agrees; batched FDTD elsewhere."""
+    """Surrogate answers where the ensemble agrees; batched FDTD elsewhere.  The
+    gate is the model's calibrated one (``Ensemble.calibrate``), else a spread
+    threshold (``threshold`` or ``THRESHOLD``)."""
     torch = model.torch
     torch.cuda.synchronize(model.device)
     t0 = time.perf_counter()
     S, spread, _ = model.predict(designs)
+    acc = model.gate(designs, spread, threshold)
     t1 = time.perf_counter()
-    acc = spread <= threshold
     fb = [d for d, a in zip(designs, acc) if not a]
     t_fdtd = 0.0
     if fb:

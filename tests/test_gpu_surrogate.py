@@ -116,29 +116,35 @@ def test_adam_step_and_training_progress(torch):
 
 def test_surrogate_gain_over_fdtd_alone(torch):
     """What the trained network adds to the batched FDTD: trained on the batched
-    FDTD's spectra of designs 0-4095, on 96 held-out couplers the pipeline
-    (ensemble answers where its spread is <= 1e-3, batched FDTD elsewhere) returns
-    every design faster than the batched FDTD alone, the answered designs within a
-    median RMS S-parameter error of 1e-3, and the fallback designs exactly as the
-    FDTD computes them.  (bench.py --workload surrogate runs the 256-design
-    held-out set and the 8192-query inference batch.)"""
+    FDTD's spectra of designs 0-4095, its gate calibrated on designs 5000-6023
+    (per coupling-length band, the largest ensemble spread at which 98 % of the
+    admitted designs are within the 1e-3 error bar), on 128 held-out couplers the pipeline (ensemble answers
+    where the spread is under the gate, batched FDTD elsewhere) returns every
+    design faster than the batched FDTD alone, at least 95 % of the answered
+    designs within an RMS S-parameter error of 1e-3, and the fallback designs
+    exactly as the FDTD computes them.  (bench.py --workload surrogate runs the
+    256-design held-out set and the 8192-query inference batch.)"""
     from prismo_gb300 import surrogate as Su
     from prismo_gb300 import sweep as S
 
     train = [S.coupler_design(s) for s in range(4096)]
-    test = [S.coupler_design(s) for s in range(10000, 10096)]
+    calib = [S.coupler_design(s) for s in Su.CALIB_SEEDS]
+    test = [S.coupler_design(s) for s in range(10000, 10128)]
     Str = np.concatenate([S.batched_sweep(train[q:q + 1024]).S for q in range(0, 4096, 1024)])
     ref = S.batched_sweep(test)  # the method without the network
     E = Su.Ensemble(max_batch=1024)
     E.fit(train, Str, epochs=Su.EPOCHS)
+    E.calibrate(calib, np.concatenate([S.batched_sweep(calib[q:q + 512]).S for q in range(0, len(calib), 512)]))
     res = Su.run_pipeline(E, test)
     err = Su.s_error(res.S, ref.S)
     acc = res.accepted
-    print(f"accepted {acc.sum()}/{len(test)}, answered err median {np.median(err[acc]):.2e} "
-          f"max {err[acc].max():.2e}; pipeline {res.seconds:.2f} s vs FDTD {ref.seconds:.2f} s")
+    within = float(np.mean(err[acc] <= 1e-3)) if acc.any() else 0.0
+    print(f"gate {E.calibration}; accepted {acc.sum()}/{len(test)}, within 1e-3 {within:.3f}, "
+          f"answered err median {np.median(err[acc]):.2e} max {err[acc].max():.2e}; "
+          f"pipeline {res.seconds:.2f} s vs FDTD {ref.seconds:.2f} s")
     assert acc.sum() >= 5
     assert np.all(err[~acc] == 0.0)
-    assert np.median(err[acc]) <= 1e-3
+    assert within >= 0.95, within
     assert res.seconds < ref.seconds
     E.close()
 
@@ -163,4 +169,32 @@ def test_tcgen05_forward_matches_mma_sync(torch):
     for m in range(E.members):
         want, _ = mlp64.forward(p[m], x[m], DIMS)
         assert rel(y1[m], want) <= 1e-2
+    E.close()
+
+
+def test_tcgen05_backward_matches_mma_sync(torch):
+    """The data- and weight-gradient products on tcgen05 against the mma.sync
+    products: the last layer's weight gradient (the first product, from the same
+    bf16 loss gradient) to float32 summation order (rel 1e-5); the layers below
+    through bf16-rounded data gradients, where an element can round the other
+    way (rel 1e-2); batch 320 leaves a partial 128-row tile."""
+    E, p, x, t = make(torch, members=2, batch=320, seed=11)
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda")
+    td = torch.tensor(t, dtype=torch.float32, device="cuda")
+    segs, _ = mlp64.layout(DIMS)
+    out = []
+    for tc in (False, True):
+        E.set_tensor_path(tc)
+        E.forward_raw(xd)
+        E.gradients_raw(xd, td)
+        out.append(E.grads())
+    assert E.status() == 0
+    g0, g1 = out
+    for m in range(E.members):
+        for l, (w_off, b_off, n, k) in enumerate(segs):
+            a, b = g1[m, w_off:w_off + n * k], g0[m, w_off:w_off + n * k]
+            assert rel(a, b) <= (1e-5 if l == 3 else 1e-2), (m, l, rel(a, b))
+        l_o, g_o = mlp64.loss_and_grads(p[m], x[m], t[m], DIMS)
+        for l, (w_off, b_off, n, k) in enumerate(segs):
+            assert rel(g1[m, w_off:w_off + n * k], g_o[w_off:w_off + n * k]) <= 3e-2, (m, l)
     E.close()
