@@ -8,8 +8,10 @@ per-frequency plane norms and sums), for the seeded couplers their complex
 S-parameters.  Each test runs the same configuration on the GPU in float32 and
 states the error against float64:
 
-* 256^3 CPML grid, 2000 steps: sampled fields rel L2 <= 1e-5 per component,
-  full-field norms within 1e-5, the probe traces within 1e-5 of their peak;
+* 256^3 CPML grid, 2000 steps: E and H, each taken as one vector, sampled
+  fields rel L2 <= 1e-5 and full-field norms within 1e-5, the Ez probe traces
+  within 1e-5 of their peak (Hz of this z-dipole is nearly zero -- only the
+  boxes break the symmetry -- so its own relative error is larger; printed);
 * 384 x 384 x 192 dispersive grid (Drude + 2 Lorentz, TFSF, two 64-frequency
   planes): E and H, each taken as one vector, <= 1e-5, DFT <= 1e-4 per sampled
   frequency.  The cross-polarised components (Ey, Ez, Hx, Hz) of this x-polarised
@@ -101,9 +103,9 @@ def test_3d_256_cpml_full_size_vs_oracle(torch):
     eng.add_source("Ez", eng.offsets("Ez", tuple(np.array([v]).reshape(1, 1, 1) for v in c)), None, wf)
     amps = np.asarray(wf((np.arange(n) + 1) * dt), dtype=np.float64).reshape(n, 1)
     trace = []
-    ez = eng.component("Ez")
     for s0 in range(0, n, every):  # the probe cells every `every` steps
         eng.step(every, amps[s0:s0 + every])
+        ez = eng.component("Ez")  # a view of the current field set (the sets alternate)
         trace.append([float(ez[tuple(p)]) for p in meta["probes"]])
     assert eng.check_status() == 0
     want = z["trace_Ez"]
@@ -112,7 +114,7 @@ def test_3d_256_cpml_full_size_vs_oracle(torch):
     terr = float((np.abs(got - want) / peak).max())
     print(f"probe traces: max |err| / peak = {terr:.2e} ({len(trace)} samples x {len(meta['probes'])} probes)")
     assert terr <= 1e-5
-    _compare_fields(lambda comp: eng.component(comp).double().cpu().numpy(), z, meta)
+    _compare_fields(lambda comp: eng.component(comp).double().cpu().numpy(), z, meta, vectors=True)
     eng.close()
 
 
