@@ -865,10 +865,29 @@ int ts_items(pc_ctx* c, TsState* st, int cx, cudaStream_t stream) {
     std::vector<int4> h;
     std::vector<float> cost;
     std::vector<int> chunk;
-    for (int ib = 0; ib < g.nx; ib += cx)
+    // x-chunk boundaries: with an x CPML the end chunks cover the slab and the K
+    // planes beyond it, so that the chunks between them (whose K halo planes then
+    // stay clear of the slab) run without x-CPML code; cx elsewhere
+    std::vector<int> bounds{0};
+    {
+        const int edge_len = t + K;
+        const bool split_ends = t > 0 && g.nx > 2 * edge_len + 2 * K;
+        int ib = 0;
+        if (split_ends) {
+            ib = edge_len;
+            bounds.push_back(ib);
+        }
+        const int stop = split_ends ? g.nx - edge_len : g.nx;
+        while (ib < stop) {
+            ib = std::min(stop, ib + cx);
+            bounds.push_back(ib);
+        }
+        if (split_ends) bounds.push_back(g.nx);
+    }
+    for (size_t ci = 0; ci + 1 < bounds.size(); ++ci)
         for (int j0 = 0; j0 < g.ny; j0 += TS_TY)
             for (int k0 = 0; k0 < g.nz; k0 += TS_TZ) {
-                const int ie = std::min(g.nx, ib + cx);
+                const int ib = bounds[ci], ie = bounds[ci + 1];
                 const int jlo = j0 - K, jhi = j0 + TS_TY + K, klo = k0 - K, khi = k0 + TS_TZ + K;
                 const int plo = ib - K, phi = ie + K;  // planes [plo, phi)
                 const bool cxs = touches_slab(plo, phi, g.nx), cys = touches_slab(jlo, jhi, g.ny),
@@ -889,14 +908,14 @@ int ts_items(pc_ctx* c, TsState* st, int cx, cudaStream_t stream) {
                 const int w = ie | (cls << 20) | ((src && st->src_ok) ? (1 << 28) : 0);
                 h.push_back(make_int4(k0, j0, ib, w));
                 cost.push_back(kCost[cls] * (float)(ie - ib + 2 * K));
-                chunk.push_back(ib / cx);
+                chunk.push_back((int)ci);
             }
     if (c->ts_order != 0) {
         // order 1: x-chunks by their summed cost, most expensive first (the slab
         // chunks), and within a chunk the slower items first; the tiles of one
         // chunk still run together (one chunk is about one wave of CTAs), so their
         // shared halo rows are read from L2.  order 2: every item by cost.
-        const int nch = (g.nx + cx - 1) / cx;
+        const int nch = (int)bounds.size() - 1;
         std::vector<float> csum(nch, 0.f);
         for (size_t q = 0; q < h.size(); ++q) csum[chunk[q]] += cost[q];
         std::vector<int> ord(h.size());
