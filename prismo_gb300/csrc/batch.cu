@@ -923,6 +923,9 @@ int pc_batch_set_cpml(pc_batch* b, const double* bcoef, const double* acoef, con
 
 int pc_batch_set_sources(pc_batch* b, const double* weights, const double* amps, int32_t namps) {
     if (!b || namps < 0 || (namps > 0 && !amps) || (b->lay.weight_elems > 0 && !weights)) return PC_ERR_INVALID;
+    // passes already queued (on any stream) may still read the tables being replaced
+    if (b->steps_done > 0) PC_CUDA_CHECK(cudaDeviceSynchronize());
+    if (namps != b->namps) drop_graphs(b);  // captured passes hold the table's address and length
     if (b->lay.weight_elems > 0)
         PC_CUDA_CHECK(cudaMemcpy(b->d_w, weights, b->lay.weight_elems * sizeof(double), cudaMemcpyHostToDevice));
     if (namps > b->namps || !b->d_amps) {

@@ -74,7 +74,8 @@ class FDTDEngine:
     def __init__(self, dims: Sequence[int], spacing: Sequence[float], dt: float, *, is_2d: bool,
                  precision: str = "fp32", mode: str = "corrected", sched: str = "auto",
                  material_arrays: Optional[dict] = None, pml: Optional[PMLParams] = None,
-                 device: str = "cuda:0", stream=None, sets=None, bind_later: bool = False):
+                 device: str = "cuda:0", stream=None, sets=None, bind_later: bool = False,
+                 batch_route: bool = True):
         torch = _torch()
         self.lib = _lib.load()
         if not torch.cuda.is_available():
@@ -130,6 +131,11 @@ class FDTDEngine:
         self.dfts = []  # (comp, offsets, omegas, accumulator tensor)
         self.fluxes = []  # per-step power histories (device float64)
         self.mode_mons = []  # per-step mode-coefficient histories (device complex128)
+        self._dft_t0 = []
+        # 2D TE simulations of the shape the batched kernel covers run on it (see _route_2d)
+        self.batch_route = bool(batch_route)
+        self._route = None
+        self._stepped = False
         self._closed = False
 
     # -- setup ---------------------------------------------------------------
@@ -170,6 +176,7 @@ class FDTDEngine:
             return t
 
         eps, mu, sig, sigm = dev("eps_rel"), dev("mu_rel"), dev("sigma_e"), dev("sigma_m")
+        self._eps_cells = eps  # the cell permittivity (device, float64), for the 2D batched route
         need_ca = sig is not None and bool(torch.any(sig != 0).item())
         need_h = (mu is not None and bool(torch.any(mu != 1).item())) or \
                  (sigm is not None and bool(torch.any(sigm != 0).item()))
@@ -227,6 +234,8 @@ class FDTDEngine:
 
     @property
     def cur(self) -> int:
+        if self._route is not None:
+            return self._route.cur
         return int(self.lib.pc_current_set(self.ctx))
 
     def component(self, comp: str, set_index: Optional[int] = None):
@@ -257,6 +266,7 @@ class FDTDEngine:
             self.ctx, COMP_INDEX[comp], offs.ctypes.data_as(C.POINTER(C.c_int64)),
             None if w is None else w.ctypes.data_as(C.POINTER(C.c_double)), int(offs.size)), "pc_add_source")
         self.sources.append((comp, offs, w, waveform))
+        self._route_check("add_source")
         return sid
 
     # -- dispersive regions ----------------------------------------------------------
@@ -318,10 +328,15 @@ class FDTDEngine:
             om.ctypes.data_as(C.POINTER(C.c_double)), int(om.size), self.dt, float(t0), acc.data_ptr()),
             "pc_add_dft")
         self.dfts.append((comp, offs, om, acc))
+        self._dft_t0.append(float(t0))
+        self._route_check("add_dft")
         return mid
 
     def dft_result(self, mid: int):
         """Complex (nf, npts) accumulator of a DFT monitor (flushes pending samples)."""
+        if self._route is not None:
+            torch = _torch()
+            return torch.as_tensor(self._route.spectra()[0][mid], device=self.device)
         _lib.check(self.lib.pc_dft_flush(self.ctx, int(mid), self._stream_ptr()), "pc_dft_flush")
         acc = self.dfts[mid][3].double()
         return torch_complex(acc[..., 0] - acc[..., 2], acc[..., 1] - acc[..., 3])
@@ -400,6 +415,12 @@ class FDTDEngine:
     def step(self, nsteps: int = 1, amps: Optional[np.ndarray] = None):
         """Advance nsteps; amps[nsteps, nsources] are the source amplitudes at
         t_{n+1} of each step (sources/point.py:62-73)."""
+        if self._route is None and not self._stepped and self.batch_route:
+            self._route = self._route_2d()
+        self._stepped = True
+        if self._route is not None:
+            self._route.step(int(nsteps), amps)
+            return
         ns = len(self.sources) + (1 if getattr(self, "tfsf", None) is not None else 0)
         ap = None
         if ns:
@@ -411,7 +432,74 @@ class FDTDEngine:
     def status(self) -> int:
         v = C.c_uint32(0)
         _lib.check(self.lib.pc_status(self.ctx, C.byref(v), self._stream_ptr()), "pc_status")
-        return int(v.value)
+        return int(v.value) | (self._route.status() if self._route is not None else 0)
+
+    # -- the 2D batched route ------------------------------------------------------
+    def _route_2d(self):
+        """A one-instance batched run (csrc/batch.cu: K time steps per launch in
+        shared memory) of this engine's own Ez, Hx, Hy buffers, when the
+        simulation has the shape that kernel covers: 2D, float32, corrected
+        stepper, lossless non-magnetic media, dx = dy, the default CPML profile,
+        at most one soft Ez source on one x column over consecutive y, at most
+        four Ez DFT lines of that form sharing their frequencies and first sample
+        time, no flux or mode monitors, and the Hz family (Ex, Ey, Hz) zero.
+        Decided at the first step; returns None when the shape does not fit."""
+        if not (self.is_2d and self.precision == "fp32" and self.mode == _lib.PC_MODE_CORRECTED):
+            return None
+        if self.has_ca or self.has_hcoef or getattr(self, "tfsf", None) is not None or self.fluxes or \
+                self.mode_mons or getattr(self, "ade_aux", None):
+            return None
+        if self.spacing[0] != self.spacing[1] or len(self.sources) > 1 or len(self.dfts) > 4:
+            return None
+        t = 0 if self.pml is None else int(self.pml.thickness)
+        if self.pml is not None and self.pml != PMLParams(thickness=t):
+            return None
+        if any(float(self.component(c).abs().max()) != 0.0 for c in ("Ex", "Ey", "Hz")):
+            return None
+
+        def line(offs):
+            x, y = offs // self.pitch, offs % self.pitch
+            if offs.size == 0 or np.any(x != x[0]) or np.any(y != y[0] + np.arange(offs.size)):
+                return None
+            return int(x[0]), int(y[0]), int(offs.size)
+
+        from . import sweep as SW
+
+        if self.sources:
+            comp, offs, w, _ = self.sources[0]
+            ln = line(offs)
+            if comp != "Ez" or ln is None:
+                return None
+            src = SW.Port(ln[0], ln[1], ln[2], np.ones(ln[2]) if w is None else np.asarray(w, dtype=np.float64))
+        else:
+            src = SW.Port(1, 1, 0, np.zeros(0))
+        ports = []
+        for q, (comp, offs, om, _) in enumerate(self.dfts):
+            ln = line(offs)
+            if comp != "Ez" or ln is None or not np.array_equal(om, self.dfts[0][2]) or \
+                    self._dft_t0[q] != self._dft_t0[0]:
+                return None
+            ports.append(SW.Port(ln[0], ln[1], ln[2], np.ones(ln[2])))
+        nx, ny = self.dims[0], self.dims[1]
+        if nx < 2 * t + 4 or ny < 2 * t + 4:
+            return None
+        eps = self._eps_cells
+        eps = np.ones((nx, ny)) if eps is None else eps.reshape(nx, ny).double().cpu().numpy()
+        torch = _torch()
+        # the batch steps components 2-4 (Ez, Hx, Hy) of the engine's set buffers
+        # in place, ping-pong between them: a second set joins the engine's
+        if len(self.sets) < 2:
+            self.sets.append(torch.zeros_like(self.sets[0]))
+        freqs = self.dfts[0][2] / (2 * np.pi) if self.dfts else np.array([1.0])
+        return _Route2D(self, SW.BatchedFDTD2D(
+            [SW.Instance(np.ascontiguousarray(eps), src, ports)], freqs, dx=self.spacing[0], dt=self.dt, cpml=t,
+            device=self.device, stream=self.stream, field_sets=[s_[2:5] for s_ in self.sets[:2]],
+            dft_t0=self._dft_t0[0] if self.dfts else None))
+
+    def _route_check(self, what):
+        if self._route is not None:
+            raise RuntimeError(f"{what} after the first step of a simulation on the 2D batched route; "
+                               "create the engine with batch_route=False to change it between steps")
 
     def check_status(self):
         st = self.status()
@@ -580,12 +668,15 @@ class FDTDEngine:
         _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_GRAPH_STEPS, int(n)), "pc_set_tuning")
 
     def launch_count(self) -> int:
-        return int(self.lib.pc_launch_count(self.ctx))
+        return int(self.lib.pc_launch_count(self.ctx)) + (self._route.launches if self._route is not None else 0)
 
     def synchronize(self):
         self.stream.synchronize()
 
     def close(self):
+        if self._route is not None:
+            self._route.close()
+            self._route = None
         if not self._closed and self.ctx:
             try:
                 self.synchronize()
@@ -599,3 +690,40 @@ class FDTDEngine:
             self.close()
         except Exception:
             pass
+
+
+class _Route2D:
+    """The 2D batched route of an FDTDEngine: a one-instance BatchedFDTD2D on the
+    engine's buffers, fed the engine's per-call amplitude rows (the batch indexes
+    its amplitude table by the step count since it was set up)."""
+
+    def __init__(self, eng, batch):
+        self.eng = eng
+        self.B = batch
+        eng.psi = list(batch.psi)  # zeroing the engine's psi resets the batch's
+        self.amps = np.zeros(0)
+
+    @property
+    def cur(self) -> int:
+        return self.B.cur
+
+    @property
+    def launches(self) -> int:
+        return self.B.launches
+
+    def step(self, nsteps, amps):
+        done = self.B.steps_done
+        col = np.zeros(nsteps) if amps is None or not len(self.eng.sources) else \
+            np.asarray(amps, dtype=np.float64).reshape(nsteps, -1)[:, 0]
+        self.amps = np.concatenate([self.amps[:done], col])
+        self.B.set_amplitudes(self.amps)
+        self.B.step(nsteps)
+
+    def spectra(self):
+        return self.B.spectra()
+
+    def status(self) -> int:
+        return self.B.status()
+
+    def close(self):
+        self.B.close()

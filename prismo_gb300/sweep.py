@@ -319,7 +319,11 @@ class BatchedFDTD2D:
 
     def __init__(self, instances: Sequence[Instance], freqs, dx: float = DX, dt: Optional[float] = None,
                  cpml: int = CPML, device=None, stream=None, autotune: bool = True, graph_steps: int = 80,
-                 variant: Optional[int] = None):
+                 variant: Optional[int] = None, field_sets=None, dft_t0: Optional[float] = None):
+        """``field_sets`` (one instance only): two float32 tensors whose storage
+        from their first element holds that instance's Ez, Hx, Hy ([3][nx][pitch],
+        pitch = ny rounded up to 32) -- the batch steps them in place instead of
+        buffers of its own.  ``dft_t0``: time of the first DFT sample (default dt)."""
         import torch
 
         self.torch = torch
@@ -350,7 +354,15 @@ class BatchedFDTD2D:
         lay = self.lay
         dev, f32 = self.device, torch.float32
         with torch.cuda.device(dev):
-            self.sets = [torch.zeros(lay.field_elems, dtype=f32, device=dev) for _ in range(2)]
+            if field_sets is not None:
+                if n != 1 or len(field_sets) != 2 or any(t.dtype != f32 or not t.is_contiguous() or
+                                                          t.numel() < lay.field_elems for t in field_sets):
+                    self.lib.pc_batch_destroy(h)
+                    self.h = None
+                    raise ValueError("external field sets: one instance, two contiguous float32 tensors")
+                self.sets = list(field_sets)
+            else:
+                self.sets = [torch.zeros(lay.field_elems, dtype=f32, device=dev) for _ in range(2)]
             self.cb = torch.zeros(lay.coef_elems, dtype=f32, device=dev)
             self.psi = [torch.zeros(lay.psi_elems, dtype=f32, device=dev) for _ in range(2)]
             self.acc = torch.zeros((len(self.freqs), lay.dft_points, 4), dtype=f32, device=dev)
@@ -385,8 +397,10 @@ class BatchedFDTD2D:
                                                   ks.ctypes.data_as(D)), "pc_batch_set_cpml")
         self._w = np.ascontiguousarray(np.concatenate([I.src.profile for I in self.instances]), dtype=np.float64)
         om = np.ascontiguousarray(2 * np.pi * self.freqs)
-        _lib.check(self.lib.pc_batch_set_dft(h, om.ctypes.data_as(C.POINTER(C.c_double)), int(om.size), self.dt,
-                                             self.acc.data_ptr()), "pc_batch_set_dft")
+        if lay.dft_points > 0:
+            _lib.check(self.lib.pc_batch_set_dft(h, om.ctypes.data_as(C.POINTER(C.c_double)), int(om.size),
+                                                 self.dt if dft_t0 is None else float(dft_t0), self.acc.data_ptr()),
+                       "pc_batch_set_dft")
         self.set_amplitudes(np.zeros(0))
         self.tuning_ms = None
         if variant is not None:
@@ -458,6 +472,12 @@ class BatchedFDTD2D:
     @property
     def cur(self) -> int:
         return int(self.lib.pc_batch_current_set(self.h))
+
+    def status(self) -> int:
+        """The batch's PC_STATUS_* word."""
+        v = C.c_uint32(0)
+        _lib.check(self.lib.pc_batch_status(self.h, C.byref(v), self.stream.cuda_stream), "pc_batch_status")
+        return int(v.value)
 
     def instance_status(self) -> np.ndarray:
         """Per-instance PC_STATUS_* words since the last read (then cleared):

@@ -99,3 +99,39 @@ def test_3d_fp32_workload_full_size_vs_fp64(torch):
     print("fp32 vs fp64 rel L2 after 2000 steps:", errs)
     for k in COMPS:
         assert errs[k] <= 1e-5, (k, errs[k])
+
+
+def test_2d_config_batched_route_equals_engine_kernels(torch):
+    """The 2D TE configuration through FDTDEngine runs on the batched kernel
+    (K time steps per launch); the same engine with that route off runs the
+    per-step kernels: the two float32 paths round differently (explicit
+    roundings against contracted multiply-adds) and agree to 1e-5 in the fields
+    and the DFT line, the bar both meet against the float64 oracle."""
+    from prismo_gb300.engine import FDTDEngine
+    from prismo_gb300.pml import PMLParams
+    from prismo_gb300.workloads import CONFIG_2D, config_2d_layout
+
+    cfg = CONFIG_2D
+    g = O.OracleGrid.from_total(*cfg["dims"], cfg["dx"], cfg["cpml"])
+    dt = g.suggest_dt(cfg["courant"])
+    eps, src, mon, freqs = config_2d_layout()
+    wf = O.gaussian_pulse(cfg["pulse_f0"], cfg["pulse_width"])
+    n = cfg["steps"]
+    amps = np.array([wf(x) for x in np.cumsum(np.full(n, dt))])[:, None]
+    out = []
+    for route in (False, True):
+        eng = FDTDEngine(g.dims, g.spacing, dt, is_2d=True, precision="fp32", material_arrays={"eps_rel": eps},
+                         pml=PMLParams(thickness=cfg["cpml"]), batch_route=route)
+        eng.add_source("Ez", eng.offsets("Ez", src), None, wf)
+        m = eng.add_dft("Ez", eng.offsets("Ez", mon), freqs, t0=dt)
+        eng.step(n // 2, amps[: n // 2])  # two calls: the amplitude rows continue
+        eng.step(n - n // 2, amps[n // 2:])
+        assert (eng._route is not None) == route
+        assert eng.check_status() == 0
+        out.append(({c: eng.component(c).double().cpu().numpy() for c in ("Ez", "Hx", "Hy")},
+                    eng.dft_result(m).cpu().numpy(), eng.launch_count()))
+        eng.close()
+    for c in ("Ez", "Hx", "Hy"):
+        assert rel(out[1][0][c], out[0][0][c]) <= 1e-5, (c, rel(out[1][0][c], out[0][0][c]))
+    assert rel(out[1][1], out[0][1]) <= 1e-5
+    print("launches: per-step kernels", out[0][2], "batched route", out[1][2])

@@ -277,7 +277,7 @@ def test_captured_time_loop_matches_eager_steps(torch, is2d):
     outs = []
     for graph_steps in (0, 64):
         eng = make_engine(g.dims, g.spacing, dt, is2d, precision="fp32", material_arrays=mats,
-                          pml=PMLParams(thickness=6 if not is2d else 8))
+                          pml=PMLParams(thickness=6 if not is2d else 8), batch_route=False)
         eng.set_graph_steps(graph_steps)
         eng.add_source(comp, eng.offsets(comp, idx), None, wf)
         m = eng.add_dft(comp, eng.offsets(comp, mon), freqs, t0=dt)
