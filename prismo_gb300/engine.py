@@ -491,10 +491,13 @@ class FDTDEngine:
         if len(self.sets) < 2:
             self.sets.append(torch.zeros_like(self.sets[0]))
         freqs = self.dfts[0][2] / (2 * np.pi) if self.dfts else np.array([1.0])
+        # one instance: the 32 x 64 tile with 4 steps per pass (the variant the
+        # tuner picks for a single 500 x 250 grid), without timing every variant
+        variant = next((v for v, tv in enumerate(SW.BatchedFDTD2D.variants()) if tuple(tv) == (32, 64, 4)), 1)
         return _Route2D(self, SW.BatchedFDTD2D(
             [SW.Instance(np.ascontiguousarray(eps), src, ports)], freqs, dx=self.spacing[0], dt=self.dt, cpml=t,
             device=self.device, stream=self.stream, field_sets=[s_[2:5] for s_ in self.sets[:2]],
-            dft_t0=self._dft_t0[0] if self.dfts else None))
+            dft_t0=self._dft_t0[0] if self.dfts else None, autotune=False, variant=variant))
 
     def _route_check(self, what):
         if self._route is not None:
