@@ -669,6 +669,7 @@ def run_sweep(args, cpu, peak, peak_kind):
     # end to end from the design list (layouts included) once more
     e2e = S.batched_sweep(designs, variant=variant)
     ser = S.serial_sweep(designs[:2])
+    ser_k = S.serial_sweep(designs[:2], batch_route=False)
     err = float(np.abs(timed[-1].S[:2] - ser.S).max())
     # the batch kernel's roofline: unblocked 2D bytes per cell update (28 B + CPML edges)
     bpc = 28.0 + 16.0 * float(np.mean([(2 * S.CPML / I.eps.shape[0] + 2 * S.CPML / I.eps.shape[1])
@@ -685,6 +686,8 @@ def run_sweep(args, cpu, peak, peak_kind):
               sum(I.eps.nbytes for I in S.instances_for(layouts))), "d2h_bytes_per_step": int(
               e2e.S.size * 16), "api": "prismo_gb300.sweep.batched_sweep (design list in, S-parameters out)"},
           serial_designs_per_s=ser.designs_per_s, batched_vs_serial=(args.designs / e2e.seconds) / ser.designs_per_s,
+          serial_per_step_kernels_designs_per_s=ser_k.designs_per_s,
+          batched_vs_serial_per_step_kernels=(args.designs / e2e.seconds) / ser_k.designs_per_s,
           max_abs_S_batched_vs_serial=err,
           roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                     "peak_kind": peak_kind, "traffic": None, "bytes_per_cell_update": bpc,
@@ -717,6 +720,7 @@ def run_surrogate(args, cpu):
     err = Su.s_error(res.S, ref.S)
     acc = res.accepted
     ser = S.serial_sweep(test[:4])
+    ser_k = S.serial_sweep(test[:4], batch_route=False)
     # inference on a batch of 8192 queries (host features + device forward + re-embedding)
     q = [S.coupler_design(s) for s in range(20000, 20000 + 8192)]
     E.predict(q[:64])
@@ -763,6 +767,8 @@ def run_surrogate(args, cpu):
           err_rms_all_max=float(err.max()),
           batched_fdtd_designs_per_s=r_fdtd, serial_designs_per_s=ser.designs_per_s,
           pipeline_vs_serial=res.designs_per_s / ser.designs_per_s,
+          serial_per_step_kernels_designs_per_s=ser_k.designs_per_s,
+          pipeline_vs_serial_per_step_kernels=res.designs_per_s / ser_k.designs_per_s,
           inference={"queries": 8192, "seconds": t_inf, "designs_per_s": 8192 / t_inf,
                      "accept_fraction": float(np.mean(E.gate(q, spread_q))),
                      "device_forward_ms": fwd_ms, "device_tflops": flops / (fwd_ms * 1e-3) / 1e12,

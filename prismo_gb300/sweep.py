@@ -594,17 +594,19 @@ def batched_sweep(designs: Sequence[CouplerDesign], nsteps: int = STEPS, nfreq: 
 
 
 def serial_sweep(designs: Sequence[CouplerDesign], nsteps: int = STEPS, nfreq: int = NFREQ, device=None,
-                 layouts=None, warm: bool = True) -> SweepResult:
+                 layouts=None, warm: bool = True, batch_route: bool = True) -> SweepResult:
     """The plain path: one single-simulation 2D engine per coupler and per
     normalisation run, one after another (ParameterSweep's sequential loop).
-    Timed like ``batched_sweep``: from the design list to the S-parameters."""
+    Timed like ``batched_sweep``: from the design list to the S-parameters.
+    ``batch_route``: the engine's 2D batched route (K steps per launch) or its
+    per-step kernels."""
     import torch
 
     from .engine import FDTDEngine
 
     dev = torch.device(device or "cuda")
     if warm:  # one short untimed run: library load, first-launch and allocator warm-up
-        serial_sweep(designs[:1], nsteps=16, nfreq=nfreq, device=device, warm=False)
+        serial_sweep(designs[:1], nsteps=16, nfreq=nfreq, device=device, warm=False, batch_route=batch_route)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     layouts = layouts or [coupler_layout(d) for d in designs]
@@ -619,7 +621,8 @@ def serial_sweep(designs: Sequence[CouplerDesign], nsteps: int = STEPS, nfreq: i
         for eps, ports in ((L.eps, L.ports), (L.norm_eps, L.ports[:1])):
             nx, ny = eps.shape
             eng = FDTDEngine((nx, ny, 1), (DX, DX, DX), dt, is_2d=True, precision="fp32",
-                             material_arrays={"eps_rel": eps[:, :, None]}, pml=PMLParams(CPML), device=dev)
+                             material_arrays={"eps_rel": eps[:, :, None]}, pml=PMLParams(CPML), device=dev,
+                             batch_route=batch_route)
             idx = (np.array([[L.src.x]]), np.arange(L.src.y0, L.src.y0 + L.src.n)[None, :])
             eng.add_source("Ez", eng.offsets("Ez", idx), L.src.profile, None)
             ids = []
