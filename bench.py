@@ -229,6 +229,10 @@ def run_reference(args):
     el = time.perf_counter() - t0
     cells = float(np.prod(dims))
     value = cells * per * args.steps / el / 1e9
+    # the unmodified reference stepper (MaxwellUpdater.step, core/solver.py:535-552,
+    # imported from the installed copy under baseline/_ref): no CPML, and unstable,
+    # so only its time per step on the same grid is reported
+    l0 = reference_l0_timing(dims, eps, dt)
     line = {
         "impl": "reference", "metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
@@ -238,8 +242,52 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": "Gcell/s", "cores": 1, "kind": "port",
                          "sample": f"{per} of 2000 time steps per bench step, NumPy float64 oracle, 1 thread"},
         "e2e": {"value": value, "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_stepper_l0": l0,
     }
     print(json.dumps(line), flush=True)
+
+
+def reference_l0_timing(dims, eps, dt, steps=2):
+    """Time per step of the unmodified reference MaxwellUpdater on this grid (the
+    reference package installed under baseline/_ref), or why it could not run."""
+    import builtins
+    import types
+
+    path = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(path, "prismo")):
+        return {"unavailable": "reference package not installed under baseline/_ref"}
+    try:
+        builtins.MTLBuffer = object  # the reference's metal backend annotates with it unguarded
+        pl = types.ModuleType("polars")
+        pl.DataFrame = object
+        sys.modules.setdefault("polars", pl)
+        try:  # a dependency of the reference's sweep module only, absent on some machines
+            import tqdm  # noqa: F401
+        except ImportError:
+            tq = types.ModuleType("tqdm")
+            tq.tqdm = lambda it=None, *a, **k: it
+            sys.modules["tqdm"] = tq
+        if path not in sys.path:
+            sys.path.insert(0, path)
+        from prismo.core.fields import ElectromagneticFields
+        from prismo.core.grid import GridSpec, YeeGrid
+        from prismo.core.solver import MaxwellUpdater
+
+        n = dims[0]
+        size = tuple((d - 2 * CPML - 0.5) * DX for d in dims)
+        grid = YeeGrid(GridSpec(size=size, resolution=1.0 / DX, boundary_layers=CPML))
+        upd = MaxwellUpdater(grid, dt, material_arrays={"eps_rel": eps})
+        fields = ElectromagneticFields(grid)
+        upd.step(fields)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            upd.step(fields)
+        el = (time.perf_counter() - t0) / steps
+        return {"value": float(np.prod(grid.dimensions)) / el / 1e9, "unit": "Gcell/s", "ms_per_step": el * 1e3,
+                "cores": 1, "grid": list(grid.dimensions), "steps_timed": steps,
+                "api": "prismo.core.solver.MaxwellUpdater.step (unmodified; no CPML)", "n": n}
+    except Exception as e:  # noqa: BLE001 - report, never fail the bench line
+        return {"unavailable": f"{type(e).__name__}: {e}"[:200]}
 
 
 def main():
@@ -626,6 +674,7 @@ def run_dispersive(args, peak, peak_kind):
     cells = float(np.prod(dims))
     value = cells * per * args.steps / (ms / 1e3) / 1e9
     bpc = dispersive_bytes_per_cell(dims, 12, info["box"], 2, len(info["planes"]), len(info["freqs"]))
+    bpc_ring = dispersive_bytes_per_cell(dims, 12, info["box"], 2, len(info["planes"]), len(info["freqs"]), "ring")
     avg = kern_ms / 1e3 / max(kern_n, 1)
     ach = bpc * cells / avg / 1e9
     _line(metric="Gcell-updates/s", value=value, unit="Gcell/s", steps=args.steps, warmup=args.warmup,
@@ -636,7 +685,8 @@ def run_dispersive(args, peak, peak_kind):
           roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                     "peak_kind": peak_kind, "traffic": _profile_value("dispersive_384.json", dims,
                                                                         "dram_bytes_per_step"),
-                    "bytes_per_cell_update": bpc,
+                    "bytes_per_cell_update": bpc, "frac_ring_model": bpc_ring * cells / avg / 1e9 / peak,
+                    "bytes_per_cell_update_ring_model": bpc_ring,
                     "kernel": "split H + E(ADE) + TFSF stencil per step", "avg_launch_us": avg * 1e6},
           gpu_launches=eng.launch_count() - n0, clocks=clk)
     eng.close()
