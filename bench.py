@@ -312,6 +312,8 @@ def main():
                          "64-frequency DFT planes; sweep: 64 batched couplers; surrogate: train + held-out pipeline; "
                          "mlp: the surrogate's forward products alone (tcgen05 and mma.sync)")
     ap.add_argument("--designs", type=int, default=64, help="designs per batched sweep")
+    ap.add_argument("--dispersive-schedule", default="fused", choices=["fused", "split"],
+                    help="dispersive workload: fused H + E kernel with the ADE pole pass, or the split kernels")
     args = ap.parse_args()
     if args.workload != "3d":
         return run_other(args)
@@ -645,6 +647,15 @@ def run_dispersive(args, peak, peak_kind):
     dims = CONFIG_3D_DISPERSIVE["dims"]
     per = args.tsteps if args.tsteps != TSTEPS else 400
     eng, info = build_dispersive_engine(dims)
+    fused = args.dispersive_schedule == "fused"
+    eng.set_fused_extras(fused)
+    tuned = None
+    if fused and args.chunk:  # fixed x-chunks (profiling runs)
+        cx, _, ce = args.chunk.partition(",")
+        eng.set_chunk(int(cx), int(ce or 0))
+        tuned = [int(cx), int(ce or 0)]
+    elif fused and not args.no_autotune:
+        tuned = eng.autotune(cache=False)
     total = (args.warmup + args.steps) * per
     amps = info["waveform"]((np.arange(total) + 1) * info["dt"])[:, None]
     pos = 0
@@ -681,13 +692,18 @@ def run_dispersive(args, peak, peak_kind):
           ms_per_step=ms / args.steps, dtype="f32",
           config={"workload": "3d_dispersive_384x384x192: Drude + 2 Lorentz half-space metal, Si3N4 ridge, TFSF "
                               "plane wave (-z, Ex), two 64-frequency Ex DFT planes, 12-cell CPML",
-                  "time_steps_per_step": per, "status": status, "l2": "inputs larger than L2"},
+                  "time_steps_per_step": per, "status": status, "l2": "inputs larger than L2",
+                  "schedule": args.dispersive_schedule, "tuned_chunk": tuned},
           roofline={"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                    "peak_kind": peak_kind, "traffic": _profile_value("dispersive_384.json", dims,
-                                                                        "dram_bytes_per_step"),
+                    "peak_kind": peak_kind,
+                    "traffic": _profile_value("fused_dispersive_384.json" if fused else "dispersive_384.json", dims,
+                                              "dram_bytes_per_step"),
                     "bytes_per_cell_update": bpc, "frac_ring_model": bpc_ring * cells / avg / 1e9 / peak,
                     "bytes_per_cell_update_ring_model": bpc_ring,
-                    "kernel": "split H + E(ADE) + TFSF stencil per step", "avg_launch_us": avg * 1e6},
+                    "kernel": ("TFSF line + fused3_multi (H+E, CPML, TFSF corrections, ADE partial update) + "
+                               "ade_pass3 (pole terms) per step" if fused else
+                               "split H + E(ADE) + TFSF stencil per step"),
+                    "avg_step_us": avg * 1e6},
           gpu_launches=eng.launch_count() - n0, clocks=clk)
     eng.close()
 

@@ -260,7 +260,11 @@ int64_t pc_launch_count(const pc_ctx* ctx);
  * the most expensive chunks (those on the x slabs) first and the slower items
  * of a chunk first, 2 (default) every item by its cost.  PC_TUNE_TS_ACTIVE
  * (read only): 1 when the temporally blocked stepper runs for this context's
- * current configuration. */
+ * current configuration.  PC_TUNE_FUSED_EXTRAS: 3D grids with ADE regions or a
+ * TFSF plane run on the fused schedule (1, default: the TFSF plane corrections
+ * and the ADE partial update inside the fused H + E kernel, the ADE pole terms in
+ * one pass over each region afterwards; needs the TFSF plane outside the ADE
+ * boxes' k ranges) or on the split schedule (0). */
 #define PC_TUNE_FUSED_CHUNK 1
 #define PC_TUNE_GRAPH_STEPS 2
 #define PC_TUNE_FUSED_CHUNK_EDGE 3
@@ -270,6 +274,7 @@ int64_t pc_launch_count(const pc_ctx* ctx);
 #define PC_TUNE_TS_CHUNK 7
 #define PC_TUNE_TS_ORDER 8
 #define PC_TUNE_TS_ACTIVE 9
+#define PC_TUNE_FUSED_EXTRAS 10
 int pc_set_tuning(pc_ctx* ctx, int32_t key, int64_t value);
 int64_t pc_get_tuning(const pc_ctx* ctx, int32_t key);
 

@@ -40,6 +40,7 @@ PC_TUNE_TS_STEPS = 6
 PC_TUNE_TS_CHUNK = 7
 PC_TUNE_TS_ORDER = 8
 PC_TUNE_TS_ACTIVE = 9
+PC_TUNE_FUSED_EXTRAS = 10
 
 
 class GridDesc(C.Structure):

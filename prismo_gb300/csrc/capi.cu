@@ -125,6 +125,7 @@ int pc_create(const pc_grid_desc* desc, pc_ctx** out) {
     c->graph_steps = 64;
     c->fused_split = 2;
     c->fused_unified = 1;
+    c->fused_extras = 1;
     c->ts_k = 2;  // temporally blocked stepper where it applies (pc_set_tuning)
     c->ts_order = 2;
     c->graph_gen[0] = c->graph_gen[1] = 0;
@@ -156,6 +157,7 @@ void pc_destroy(pc_ctx* c) {
     cudaFree(c->d_cpml_slab);
     cudaFree(c->tfsf.d_e1);
     cudaFree(c->tfsf.d_h1);
+    cudaFree(c->tfsf.d_inc);
     cudaFree(c->d_status);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
     for (int q = 0; q < 2; ++q)
@@ -354,6 +356,13 @@ int advance(pc_ctx* c, int n, int left, const double* tamp, cudaStream_t s) {
         rc = launch_ts_step(c, 1, n, s, &fused_sources);
     } else if (c->g.sched == PC_SCHED_FUSED && c->ade_n == 0 && !c->tfsf.on) {
         rc = launch_fused_step(c, s);
+    } else if (c->g.sched == PC_SCHED_FUSED && c->fused_extras && fused_extras_ok(c) && (tamp || !c->tfsf.on)) {
+        // ADE / TFSF on the fused schedule: the TFSF line first (incident values of
+        // this step), the fused H + E pass (ADE points get the partial update), then
+        // the ADE pole terms on the new set
+        rc = c->tfsf.on ? launch_tfsf_line(c, *tamp, s) : PC_OK;
+        if (!rc) rc = launch_fused_step(c, s, tamp);
+        if (!rc && c->ade_n > 0) rc = launch_ade_pass(c, c->cur ^ 1, c->cur, s);
     } else {
         rc = launch_split_step(c, s, tamp);
     }
@@ -565,11 +574,14 @@ int pc_set_tfsf(pc_ctx* c, int32_t k0, int32_t direction, int32_t polarization, 
     const size_t es = (size_t)c->g.precision;
     cudaFree(c->tfsf.d_e1);
     cudaFree(c->tfsf.d_h1);
+    cudaFree(c->tfsf.d_inc);
     c->tfsf = TfsfState{};
     PC_CUDA_CHECK(cudaMalloc(&c->tfsf.d_e1, aux_len * es));
     PC_CUDA_CHECK(cudaMalloc(&c->tfsf.d_h1, aux_len * es));
+    PC_CUDA_CHECK(cudaMalloc(&c->tfsf.d_inc, 2 * es));
     PC_CUDA_CHECK(cudaMemset(c->tfsf.d_e1, 0, aux_len * es));
     PC_CUDA_CHECK(cudaMemset(c->tfsf.d_h1, 0, aux_len * es));
+    PC_CUDA_CHECK(cudaMemset(c->tfsf.d_inc, 0, 2 * es));
     c->tfsf.on = true;
     c->tfsf.k0 = k0;
     c->tfsf.dir = direction;
@@ -632,6 +644,10 @@ int pc_set_tuning(pc_ctx* c, int32_t key, int64_t value) {
             if (value < 0 || value > 2) return PC_ERR_INVALID;
             c->ts_order = (int)value;
             return PC_OK;
+        case PC_TUNE_FUSED_EXTRAS:
+            if (value < 0 || value > 1) return PC_ERR_INVALID;
+            c->fused_extras = (int)value;
+            return PC_OK;
         default:
             return PC_ERR_INVALID;
     }
@@ -648,6 +664,7 @@ int64_t pc_get_tuning(const pc_ctx* c, int32_t key) {
     if (key == PC_TUNE_TS_CHUNK) return c->ts_cx;
     if (key == PC_TUNE_TS_ORDER) return c->ts_order;
     if (key == PC_TUNE_TS_ACTIVE) return ts_eligible(c) ? 1 : 0;
+    if (key == PC_TUNE_FUSED_EXTRAS) return c->fused_extras;
     return PC_ERR_INVALID;
 }
 

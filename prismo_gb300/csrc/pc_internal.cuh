@@ -94,6 +94,8 @@ struct TfsfState {
     double cb1;
     void* d_e1;  // auxiliary E line [M] (ctx-owned)
     void* d_h1;  // auxiliary H line [M] (ctx-owned)
+    void* d_inc; // [2]: incident E at step n and incident H at n+1/2 at the plane
+                 // (written by tfsf_line for the fused schedule; ctx-owned)
 };
 
 // Geometry of the slab-only psi storage.  Axis a keeps four slots; the lower
@@ -177,6 +179,7 @@ struct pc_ctx {
     int fused_cx_edge;  // x-chunk of tiles that touch a y or z slab (0: fused_cx)
     int fused_split;    // CPML item classes: 0 general only, 1 + single-axis, 2 + two-axis (default)
     int fused_unified;  // every class in one launch (1, default) or one launch per class (0)
+    int fused_extras;   // ADE regions and TFSF planes on the fused schedule (1, default) or split (0)
     // temporally blocked stepper (stepper_ts.cu): time steps per launch (0 = off), x-chunk
     void* ts_state;
     int ts_k;
@@ -218,7 +221,12 @@ int launch_split_step(pc_ctx* c, cudaStream_t s, const double* tfsf_amp = nullpt
 int launch_tfsf_h(pc_ctx* c, cudaStream_t s);
 int launch_tfsf_e(pc_ctx* c, double amp, cudaStream_t s);
 int launch_sources(pc_ctx* c, int step_in_batch, cudaStream_t s);
-int launch_fused_step(pc_ctx* c, cudaStream_t s);
+int launch_fused_step(pc_ctx* c, cudaStream_t s, const double* tfsf_amp = nullptr);
+// The fused schedule with ADE regions and / or a TFSF plane: the stepper needs a
+// TFSF plane (if any) clear of the ADE boxes' k ranges.
+bool fused_extras_ok(const pc_ctx* c);
+int launch_tfsf_line(pc_ctx* c, double amp, cudaStream_t s);
+int launch_ade_pass(pc_ctx* c, int in_set, int out_set, cudaStream_t s);
 void destroy_fused_state(pc_ctx* c);
 int make_map(CUtensorMap* m, const void* base, const pc_grid_desc& g, int bw, int bh);
 bool ts_eligible(const pc_ctx* c);

@@ -98,46 +98,73 @@ static AdeArgs<T> make_ade_args(pc_ctx* c) {
     return A;
 }
 
+// The dispersive region holding (i, j, k): the first region whose box contains
+// it, or -1.
+template <typename T>
+__device__ __forceinline__ int ade_region_of(const AdeArgs<T>& A, int i, int j, int k) {
+    for (int r = 0; r < A.nreg; ++r) {
+        const int* b = A.box[r];
+        if (i >= b[0] && i < b[1] && j >= b[2] && j < b[3] && k >= b[4] && k < b[5]) return r;
+    }
+    return -1;
+}
+
+// First part of the ADE E update in region r: the terms of E^n and of the
+// (CPML-modified) curl.
+template <typename T>
+__device__ __forceinline__ T ade_partial(T ce, T inv, T sdt, T e0, T curl) {
+    return ce * e0 + inv * (sdt * curl);
+}
+
+// Second part: subtract the poles' terms from the partial value, advance the
+// auxiliaries of the point (offset o in the region's arrays) and return E^{n+1}.
+template <typename T>
+__device__ __forceinline__ T ade_poles(const AdeArgs<T>& A, int r, int comp, int64_t o, T e0, T acc) {
+    for (int p = 0; p < A.npoles[r]; ++p) {
+        const T a0 = A.aux[r][comp][p][0][o];
+        if (A.kind[r][p] == 0) {
+            // (C2 - 1) P + C3 P- = (C2 + C3 - 1) P - C3 D, with D = P - P-
+            const T d1 = A.aux[r][comp][p][1][o];
+            acc -= A.inv[r] * (A.c2[r][p] * a0 - A.c3[r][p] * d1);
+        } else if (A.kind[r][p] == 1) {
+            acc -= A.inv[r] * (T(0.5) * A.dt * (T(1) + A.c1[r][p]) * a0);
+        } else {
+            acc -= A.inv[r] * ((A.c1[r][p] - T(1)) * a0);
+        }
+    }
+    const T e1 = acc;
+    for (int p = 0; p < A.npoles[r]; ++p) {
+        T* x0 = A.aux[r][comp][p][0];
+        const T a0 = x0[o];
+        if (A.kind[r][p] == 0) {
+            // D+ = C0 E+ + C1 E + (C2 + C3 - 1) P - C3 D,  P+ = P + D+
+            T* x1 = A.aux[r][comp][p][1];
+            const T dn = (A.c0[r][p] * e1 + A.c1[r][p] * e0) + (A.c2[r][p] * a0 - A.c3[r][p] * x1[o]);
+            x1[o] = dn;
+            x0[o] = a0 + dn;
+        } else {
+            x0[o] = A.c1[r][p] * a0 + A.c0[r][p] * (T(0.5) * (e1 + e0));
+        }
+    }
+    return e1;
+}
+
+// Offset of (i, j, k) in the auxiliary arrays of region r (box-local, k fastest).
+template <typename T>
+__device__ __forceinline__ int64_t ade_offset(const AdeArgs<T>& A, int r, int i, int j, int k) {
+    const int* b = A.box[r];
+    return ((int64_t)(i - b[0]) * (b[3] - b[2]) + (j - b[2])) * (b[5] - b[4]) + (k - b[4]);
+}
+
 // ADE update of one E component at (i, j, k) given E^n and the (CPML-modified)
 // curl; returns true and E^{n+1} in e when the point lies in a dispersive region.
 template <typename T>
 __device__ __forceinline__ bool ade_update(const AdeArgs<T>& A, int comp, int i, int j, int k, T curl, T& e) {
-    for (int r = 0; r < A.nreg; ++r) {
-        const int* b = A.box[r];
-        if (i < b[0] || i >= b[1] || j < b[2] || j >= b[3] || k < b[4] || k >= b[5]) continue;
-        const int64_t o = ((int64_t)(i - b[0]) * (b[3] - b[2]) + (j - b[2])) * (b[5] - b[4]) + (k - b[4]);
-        const T e0 = e;
-        T acc = A.ce[r] * e0 + A.inv[r] * (A.sdt * curl);
-        for (int p = 0; p < A.npoles[r]; ++p) {
-            const T a0 = A.aux[r][comp][p][0][o];
-            if (A.kind[r][p] == 0) {
-                // (C2 - 1) P + C3 P- = (C2 + C3 - 1) P - C3 D, with D = P - P-
-                const T d1 = A.aux[r][comp][p][1][o];
-                acc -= A.inv[r] * (A.c2[r][p] * a0 - A.c3[r][p] * d1);
-            } else if (A.kind[r][p] == 1) {
-                acc -= A.inv[r] * (T(0.5) * A.dt * (T(1) + A.c1[r][p]) * a0);
-            } else {
-                acc -= A.inv[r] * ((A.c1[r][p] - T(1)) * a0);
-            }
-        }
-        const T e1 = acc;
-        for (int p = 0; p < A.npoles[r]; ++p) {
-            T* x0 = A.aux[r][comp][p][0];
-            const T a0 = x0[o];
-            if (A.kind[r][p] == 0) {
-                // D+ = C0 E+ + C1 E + (C2 + C3 - 1) P - C3 D,  P+ = P + D+
-                T* x1 = A.aux[r][comp][p][1];
-                const T dn = (A.c0[r][p] * e1 + A.c1[r][p] * e0) + (A.c2[r][p] * a0 - A.c3[r][p] * x1[o]);
-                x1[o] = dn;
-                x0[o] = a0 + dn;
-            } else {
-                x0[o] = A.c1[r][p] * a0 + A.c0[r][p] * (T(0.5) * (e1 + e0));
-            }
-        }
-        e = e1;
-        return true;
-    }
-    return false;
+    const int r = ade_region_of(A, i, j, k);
+    if (r < 0) return false;
+    const T e0 = e;
+    e = ade_poles(A, r, comp, ade_offset(A, r, i, j, k), e0, ade_partial(A.ce[r], A.inv[r], A.sdt, e0, curl));
+    return true;
 }
 
 template <typename T>

@@ -36,6 +36,22 @@ struct FusedMaps {
     CUtensorMap cb[3];  // Cb of the E update, staged with the fields
 };
 
+// Work the fused kernel does for dispersive regions and a TFSF plane (all zero:
+// none).  E points inside an ADE box get the partial update ade_partial (the
+// pole terms follow in ade_pass3); the TFSF plane corrections of tfsf.cu are
+// added to H at k = tf_kH and to E at k = tf_k0, from the incident values that
+// tfsf_line wrote for this step.
+template <typename T>
+struct FusedXtra {
+    int nbox;
+    int box[PC_MAX_ADE_REGIONS][6];
+    T ce[PC_MAX_ADE_REGIONS], inv[PC_MAX_ADE_REGIONS];
+    T sdt;
+    int tf_on, tf_kH, tf_k0, tf_pol;  // pol 0: Hy at kH and Ex at k0; 1: Hx and Ey
+    T tf_sgn;
+    const T* tf_inc;  // [2]: incident E at step n, incident H at n+1/2
+};
+
 namespace {
 
 constexpr uint32_t kWaitLimit = 1u << 22;
@@ -92,7 +108,7 @@ enum { CL_PLAIN, CL_GEN, CL_YZ, CL_XZ, CL_XY, CL_Z, CL_Y, CL_X, CL_N };
 // and tile (with halo) stay clear of the slabs of the other axes.
 template <typename T, int TY, int TZ, int S, int AX, bool HCOEF, bool CA>
 __device__ __forceinline__ void fused3_item(const FieldArgs<T>& a, const CpmlArgs<T>& pm, const int4 item,
-                                            const FusedMaps& maps) {
+                                            const FusedMaps& maps, const FusedXtra<T>& xt) {
     using G = FusedGeom<T, TY, TZ>;
     constexpr bool CPML = AX != 0, CX = (AX & 1) != 0, CY = (AX & 2) != 0, CZ = (AX & 4) != 0;
     constexpr int EW = G::EW, HW = G::HW, NW = G::NW;
@@ -121,6 +137,20 @@ __device__ __forceinline__ void fused3_item(const FieldArgs<T>& a, const CpmlArg
     const int t = CPML ? pm.t : 0;
     const int t2 = 2 * t;
     const T idx_ = a.inv_dx, idy = a.inv_dy, idz = a.inv_dz;
+    // dispersive regions this item's E planes [ib, ie) and tile reach; TFSF values
+    // (the region loops are unrolled so that xt is indexed statically: a dynamic
+    // index into a kernel parameter would copy it to local memory)
+    bool ade_cta = false;
+#pragma unroll
+    for (int r = 0; r < PC_MAX_ADE_REGIONS; ++r) {
+        const int* b = xt.box[r];
+        ade_cta = ade_cta || (r < xt.nbox && ib < b[1] && ie > b[0] && j0 < b[3] && j0 + TY > b[2] && k0 < b[5] &&
+                              k0 + TZ > b[4]);
+    }
+    const bool tf_h = xt.tf_on && xt.tf_kH >= k0 && xt.tf_kH <= k0 + TZ;  // incl. the helper's halo column
+    const bool tf_e = xt.tf_on && xt.tf_k0 >= k0 && xt.tf_k0 < k0 + TZ;
+    const T inc_h = tf_h ? xt.tf_inc[0] : T(0);
+    const T inc_e = tf_e ? xt.tf_inc[1] : T(0);
 
     if (helper && lane == 0) {
         for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
@@ -243,6 +273,18 @@ __device__ __forceinline__ void fused3_item(const FieldArgs<T>& a, const CpmlArg
         poyc[r] = (int)pm.axis_base[1] + (psy[r] >= 0 ? psy[r] : 0) * P32 + pk[r];
         pozc[r] = (int)pm.axis_base[2] + pj[r] * t2 + (psz[r] >= 0 ? psz[r] : 0);
     }
+    // dispersive regions holding each of the thread's (j, k) points (bit per region)
+    unsigned ade_jk[2] = {0u, 0u};
+    if (ade_cta) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int rr = 0; rr < PC_MAX_ADE_REGIONS; ++rr) {
+                const int* b = xt.box[rr];
+                if (rr < xt.nbox && pj[r] >= b[2] && pj[r] < b[3] && pk[r] >= b[4] && pk[r] < b[5])
+                    ade_jk[r] |= 1u << rr;
+            }
+    }
     if (CPML) {
         // every offset a point can form over this item's planes: x-slab entries at any
         // slab index, y/z-slab entries up to the last plane, plus the largest slot
@@ -322,6 +364,13 @@ __device__ __forceinline__ void fused3_item(const FieldArgs<T>& a, const CpmlArg
         if (ux) hx = da0 * hx - db0 * (d2 - d4);
         if (uy) hy = da1 * hy - db1 * (d5 - d0);
         if (uz) hz = da2 * hz - db2 * (d1 - d3);
+        if (tf_h && kk == xt.tf_kH) {  // TFSF plane correction (tfsf_h's ranges: the update ranges here)
+            if (xt.tf_pol == 0) {
+                if (uy) hy += xt.tf_sgn * db1 * inc_h * idz;
+            } else {
+                if (ux) hx += xt.tf_sgn * db0 * inc_h * idz;
+            }
+        }
     };
 
     bool timed_out = false;
@@ -444,9 +493,34 @@ __device__ __forceinline__ void fused3_item(const FieldArgs<T>& a, const CpmlArg
                     }
                     const int cbo = (warp + NWC * r) * TZ + lane;
                     const T cb0 = Cq[cbo], cb1 = Cq[G::CB_BOX / sizeof(T) + cbo], cb2 = Cq[2 * (G::CB_BOX / sizeof(T)) + cbo];
-                    if (ux) ex = ca0 * ex + cb0 * (d2 - d4);
-                    if (uy) ey = ca1 * ey + cb1 * (d5 - d0);
-                    if (uz) ez = ca2 * ez + cb2 * (d1 - d3);
+                    unsigned am = 0u;  // dispersive regions holding the point
+                    if (ade_cta) {
+#pragma unroll
+                        for (int rr = 0; rr < PC_MAX_ADE_REGIONS; ++rr)
+                            if (q >= xt.box[rr][0] && q < xt.box[rr][1]) am |= 1u << rr;
+                        am &= ade_jk[r];
+                    }
+                    if (am) {  // partial ADE update in the first region; ade_pass3 adds the pole terms
+                        T ce = T(0), iv = T(0);
+#pragma unroll
+                        for (int rr = PC_MAX_ADE_REGIONS - 1; rr >= 0; --rr)
+                            if (am & (1u << rr)) ce = xt.ce[rr], iv = xt.inv[rr];
+                        const T sdt = xt.sdt;
+                        if (ux) ex = ade_partial(ce, iv, sdt, ex, d2 - d4);
+                        if (uy) ey = ade_partial(ce, iv, sdt, ey, d5 - d0);
+                        if (uz) ez = ade_partial(ce, iv, sdt, ez, d1 - d3);
+                    } else {
+                        if (ux) ex = ca0 * ex + cb0 * (d2 - d4);
+                        if (uy) ey = ca1 * ey + cb1 * (d5 - d0);
+                        if (uz) ez = ca2 * ez + cb2 * (d1 - d3);
+                    }
+                    if (tf_e && k == xt.tf_k0) {  // TFSF plane correction (tfsf_e's ranges)
+                        if (xt.tf_pol == 0) {
+                            if (j <= ny - 2) ex += cb0 * inc_e * idz;
+                        } else {
+                            if (q <= nx - 2) ey += cb1 * inc_e * idz;
+                        }
+                    }
                     a.Eout[0][o] = ex;
                     a.Eout[1][o] = ey;
                     a.Eout[2][o] = ez;
@@ -480,8 +554,9 @@ __device__ __forceinline__ void fused3_item(const FieldArgs<T>& a, const CpmlArg
 // one kernel variant: items[blockIdx.x], longest first
 template <typename T, int TY, int TZ, int S, int AX, bool HCOEF, bool CA>
 __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
-    fused3(FieldArgs<T> a, CpmlArgs<T> pm, const int4* __restrict__ items, const __grid_constant__ FusedMaps maps) {
-    fused3_item<T, TY, TZ, S, AX, HCOEF, CA>(a, pm, items[blockIdx.x], maps);
+    fused3(FieldArgs<T> a, CpmlArgs<T> pm, const int4* __restrict__ items, const __grid_constant__ FusedMaps maps,
+           const FusedXtra<T> xt) {
+    fused3_item<T, TY, TZ, S, AX, HCOEF, CA>(a, pm, items[blockIdx.x], maps, xt);
 }
 
 // Every class in one launch (float32, no per-cell H or Ca coefficients): the class
@@ -489,19 +564,19 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
 template <typename T, int TY, int TZ, int S>
 __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
     fused3_multi(FieldArgs<T> a, CpmlArgs<T> pm, const int4* __restrict__ items,
-                 const __grid_constant__ FusedMaps maps) {
+                 const __grid_constant__ FusedMaps maps, const FusedXtra<T> xt) {
     int4 it = items[blockIdx.x];
     const int cls = it.w >> 24;
     it.w &= 0xFFFFFF;
     switch (cls) {
-        case CL_PLAIN: fused3_item<T, TY, TZ, S, 0, false, false>(a, pm, it, maps); break;
-        case CL_Z: fused3_item<T, TY, TZ, S, 4, false, false>(a, pm, it, maps); break;
-        case CL_Y: fused3_item<T, TY, TZ, S, 2, false, false>(a, pm, it, maps); break;
-        case CL_X: fused3_item<T, TY, TZ, S, 1, false, false>(a, pm, it, maps); break;
-        case CL_YZ: fused3_item<T, TY, TZ, S, 6, false, false>(a, pm, it, maps); break;
-        case CL_XZ: fused3_item<T, TY, TZ, S, 5, false, false>(a, pm, it, maps); break;
-        case CL_XY: fused3_item<T, TY, TZ, S, 3, false, false>(a, pm, it, maps); break;
-        default: fused3_item<T, TY, TZ, S, 7, false, false>(a, pm, it, maps); break;
+        case CL_PLAIN: fused3_item<T, TY, TZ, S, 0, false, false>(a, pm, it, maps, xt); break;
+        case CL_Z: fused3_item<T, TY, TZ, S, 4, false, false>(a, pm, it, maps, xt); break;
+        case CL_Y: fused3_item<T, TY, TZ, S, 2, false, false>(a, pm, it, maps, xt); break;
+        case CL_X: fused3_item<T, TY, TZ, S, 1, false, false>(a, pm, it, maps, xt); break;
+        case CL_YZ: fused3_item<T, TY, TZ, S, 6, false, false>(a, pm, it, maps, xt); break;
+        case CL_XZ: fused3_item<T, TY, TZ, S, 5, false, false>(a, pm, it, maps, xt); break;
+        case CL_XY: fused3_item<T, TY, TZ, S, 3, false, false>(a, pm, it, maps, xt); break;
+        default: fused3_item<T, TY, TZ, S, 7, false, false>(a, pm, it, maps, xt); break;
     }
 }
 
@@ -622,8 +697,8 @@ static void fused_items(const pc_grid_desc& g, int TY, int TZ, int cx, int cx_ed
 }
 
 template <typename T, int TY, int TZ, int S, int AX, bool HCOEF, bool CA>
-int launch_variant(cudaStream_t s, const FieldArgs<T>& a, const CpmlArgs<T>& p, const FusedMaps& maps, int smem,
-                   const int4* items, int n_items) {
+int launch_variant(cudaStream_t s, const FieldArgs<T>& a, const CpmlArgs<T>& p, const FusedMaps& maps,
+                   const FusedXtra<T>& xt, int smem, const int4* items, int n_items) {
     auto kern = fused3<T, TY, TZ, S, AX, HCOEF, CA>;
     static bool attr = false;
     if (!attr) {  // the largest size any launch asks for (CPML table for PC_MAX_CPML)
@@ -633,7 +708,7 @@ int launch_variant(cudaStream_t s, const FieldArgs<T>& a, const CpmlArgs<T>& p, 
     }
     if (n_items <= 0) return PC_OK;
     dim3 blk(TZ, TY / 2 + 1);
-    kern<<<n_items, blk, smem, s>>>(a, p, items, maps);
+    kern<<<n_items, blk, smem, s>>>(a, p, items, maps, xt);
     PC_CUDA_CHECK(cudaGetLastError());
     return PC_OK;
 }
@@ -668,8 +743,30 @@ int choose_chunk(const pc_grid_desc& g, int smem) {
     return cx;
 }
 
+template <typename T>
+FusedXtra<T> make_fused_xtra(const pc_ctx* c, bool tfsf) {
+    FusedXtra<T> x{};
+    x.nbox = c->ade_n;
+    for (int r = 0; r < c->ade_n; ++r) {
+        for (int q = 0; q < 6; ++q) x.box[r][q] = c->ade[r].box[q];
+        x.ce[r] = T(c->ade_ce[r]);
+        x.inv[r] = T(c->ade_inv[r]);
+    }
+    x.sdt = T(c->ade_sdt);
+    if (tfsf && c->tfsf.on) {
+        const TfsfState& t = c->tfsf;
+        x.tf_on = 1;
+        x.tf_pol = t.pol;
+        x.tf_k0 = t.k0;
+        x.tf_kH = t.dir > 0 ? t.k0 : t.k0 + 1;  // as in tfsf_h
+        x.tf_sgn = T(((t.pol == 0) == (t.dir > 0)) ? 1 : -1);
+        x.tf_inc = static_cast<const T*>(t.d_inc);
+    }
+    return x;
+}
+
 template <typename T, int TY, int TZ, int S>
-int fused_t(pc_ctx* c, cudaStream_t s) {
+int fused_t(pc_ctx* c, cudaStream_t s, bool tfsf) {
     using G = FusedGeom<T, TY, TZ>;
     const pc_grid_desc& g = c->g;
     FusedState* st = state_of(c);
@@ -694,7 +791,8 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
     const int in = c->cur, out = c->cur ^ 1;
     FieldArgs<T> a = make_field_args<T>(c, in, out);
     CpmlArgs<T> p = make_cpml_args<T>(c, in, out);
-    if (p.t > 0 && p.total >= ((int64_t)1 << 31)) return launch_split_step(c, s);  // 32-bit psi offsets
+    const FusedXtra<T> xt = make_fused_xtra<T>(c, tfsf);
+    if (p.t > 0 && p.total >= ((int64_t)1 << 31)) return PC_ERR_INVALID;  // 32-bit psi offsets (fused_extras_ok, advance)
     // dynamic shared memory: the stage ring, H^{n+1/2} planes and this grid's CPML table
     const int smem = fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * std::max(p.t, 1) * (int)sizeof(T);
     const bool cp = p.t > 0, hc = a.da[0] != nullptr, ca = a.ca[0] != nullptr;
@@ -778,24 +876,24 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
                                                                9 * 2 * PC_MAX_CPML * (int)sizeof(T)));
                         attr = true;
                     }
-                    fused3_multi<T, TY, TZ, S><<<n, dim3(TZ, TY / 2 + 1), smem, sq>>>(a, p, it, m);
+                    fused3_multi<T, TY, TZ, S><<<n, dim3(TZ, TY / 2 + 1), smem, sq>>>(a, p, it, m, xt);
                     PC_CUDA_CHECK(cudaGetLastError());
                 }
             } else if (q == CL_GEN) {
                 switch (kp) {
-                    case 0: rc = launch_variant<T, TY, TZ, S, 7, false, false>(sq, a, p, m, smem, it, n); break;
-                    case 1: rc = launch_variant<T, TY, TZ, S, 7, false, true>(sq, a, p, m, smem, it, n); break;
-                    case 2: rc = launch_variant<T, TY, TZ, S, 7, true, false>(sq, a, p, m, smem, it, n); break;
-                    default: rc = launch_variant<T, TY, TZ, S, 7, true, true>(sq, a, p, m, smem, it, n); break;
+                    case 0: rc = launch_variant<T, TY, TZ, S, 7, false, false>(sq, a, p, m, xt, smem, it, n); break;
+                    case 1: rc = launch_variant<T, TY, TZ, S, 7, false, true>(sq, a, p, m, xt, smem, it, n); break;
+                    case 2: rc = launch_variant<T, TY, TZ, S, 7, true, false>(sq, a, p, m, xt, smem, it, n); break;
+                    default: rc = launch_variant<T, TY, TZ, S, 7, true, true>(sq, a, p, m, xt, smem, it, n); break;
                 }
             } else if constexpr (sizeof(T) == 4) {  // split classes exist only for float, kp == 0
                 switch (q) {
-                    case CL_YZ: rc = launch_variant<T, TY, TZ, S, 6, false, false>(sq, a, p, m, smem, it, n); break;
-                    case CL_XZ: rc = launch_variant<T, TY, TZ, S, 5, false, false>(sq, a, p, m, smem, it, n); break;
-                    case CL_XY: rc = launch_variant<T, TY, TZ, S, 3, false, false>(sq, a, p, m, smem, it, n); break;
-                    case CL_Z: rc = launch_variant<T, TY, TZ, S, 4, false, false>(sq, a, p, m, smem, it, n); break;
-                    case CL_Y: rc = launch_variant<T, TY, TZ, S, 2, false, false>(sq, a, p, m, smem, it, n); break;
-                    default: rc = launch_variant<T, TY, TZ, S, 1, false, false>(sq, a, p, m, smem, it, n); break;
+                    case CL_YZ: rc = launch_variant<T, TY, TZ, S, 6, false, false>(sq, a, p, m, xt, smem, it, n); break;
+                    case CL_XZ: rc = launch_variant<T, TY, TZ, S, 5, false, false>(sq, a, p, m, xt, smem, it, n); break;
+                    case CL_XY: rc = launch_variant<T, TY, TZ, S, 3, false, false>(sq, a, p, m, xt, smem, it, n); break;
+                    case CL_Z: rc = launch_variant<T, TY, TZ, S, 4, false, false>(sq, a, p, m, xt, smem, it, n); break;
+                    case CL_Y: rc = launch_variant<T, TY, TZ, S, 2, false, false>(sq, a, p, m, xt, smem, it, n); break;
+                    default: rc = launch_variant<T, TY, TZ, S, 1, false, false>(sq, a, p, m, xt, smem, it, n); break;
                 }
             } else {
                 rc = PC_ERR_INVALID;
@@ -808,10 +906,10 @@ int fused_t(pc_ctx* c, cudaStream_t s) {
     // the plain class (no CPML code) on the caller's stream
     const int4* it_plain = st->d_items + st->off_cls[CL_PLAIN];
     switch (kp) {
-        case 0: rc = launch_variant<T, TY, TZ, S, 0, false, false>(s, a, p, m, smem, it_plain, n_plain); break;
-        case 1: rc = launch_variant<T, TY, TZ, S, 0, false, true>(s, a, p, m, smem, it_plain, n_plain); break;
-        case 2: rc = launch_variant<T, TY, TZ, S, 0, true, false>(s, a, p, m, smem, it_plain, n_plain); break;
-        default: rc = launch_variant<T, TY, TZ, S, 0, true, true>(s, a, p, m, smem, it_plain, n_plain); break;
+        case 0: rc = launch_variant<T, TY, TZ, S, 0, false, false>(s, a, p, m, xt, smem, it_plain, n_plain); break;
+        case 1: rc = launch_variant<T, TY, TZ, S, 0, false, true>(s, a, p, m, xt, smem, it_plain, n_plain); break;
+        case 2: rc = launch_variant<T, TY, TZ, S, 0, true, false>(s, a, p, m, xt, smem, it_plain, n_plain); break;
+        default: rc = launch_variant<T, TY, TZ, S, 0, true, true>(s, a, p, m, xt, smem, it_plain, n_plain); break;
     }
     if (rc) return rc;
     if (fork)
@@ -921,7 +1019,7 @@ int noalloc_run(int dev, const pc_grid_desc& g, void* const set0[6], void* const
             a.Eout[q] = static_cast<T*>(Fo[q]);
             a.Hout[q] = static_cast<T*>(Fo[3 + q]);
         }
-        kern<<<nitems, dim3(TZ, TY / 2 + 1), smem, s>>>(a, pm, items, maps[cur]);
+        kern<<<nitems, dim3(TZ, TY / 2 + 1), smem, s>>>(a, pm, items, maps[cur], FusedXtra<T>{});
         PC_CUDA_CHECK(cudaGetLastError());
         cur ^= 1;
     }
@@ -970,10 +1068,29 @@ extern "C" int pc_fused_steps_noalloc(const pc_grid_desc* d, void* const set0[6]
     return rc;
 }
 
-int launch_fused_step(pc_ctx* c, cudaStream_t s) {
+bool fused_extras_ok(const pc_ctx* c) {
+    const pc_grid_desc& g = c->g;
+    if (g.ndim != 3 || g.mode != PC_MODE_CORRECTED || !c->F[1][0]) return false;
+    if (c->cpml_t > 0 && psi_layout(g, c->cpml_t).total >= ((int64_t)1 << 31)) return false;
+    if (c->tfsf.on) {
+        if (!c->tfsf.d_inc) return false;
+        const int k0 = c->tfsf.k0, kH = c->tfsf.dir > 0 ? k0 : k0 + 1;
+        if (k0 < 0 || k0 > g.nz - 2 || kH < 1 || kH > g.nz - 2) return false;
+        for (int r = 0; r < c->ade_n; ++r)  // the E correction must not precede a pole pass
+            if (k0 >= c->ade[r].box[4] && k0 < c->ade[r].box[5]) return false;
+    }
+    return true;
+}
+
+int launch_fused_step(pc_ctx* c, cudaStream_t s, const double* tfsf_amp) {
     if (c->g.ndim != 3) return launch_split_step(c, s);
-    if (c->g.precision == 8) return fused_t<double, 16, 32, 3>(c, s);
-    return fused_t<float, 16, 32, 4>(c, s);
+    if (c->cpml_t > 0 && psi_layout(c->g, c->cpml_t).total >= ((int64_t)1 << 31)) {  // 32-bit psi offsets
+        if (c->ade_n > 0 || c->tfsf.on) return PC_ERR_INVALID;
+        return launch_split_step(c, s);
+    }
+    const bool tfsf = c->tfsf.on && tfsf_amp != nullptr;
+    if (c->g.precision == 8) return fused_t<double, 16, 32, 3>(c, s, tfsf);
+    return fused_t<float, 16, 32, 4>(c, s, tfsf);
 }
 
 void destroy_fused_state(pc_ctx* c) {

@@ -11,6 +11,8 @@
 // makes the discrete curl pair adjoint; psi <- b psi + a d is the Roden-Gedney
 // recursion with the boundaries/pml.py:117-257 profiles.  The E passes set
 // PC_STATUS_NONFINITE in the status word when a value they write is NaN or Inf.
+#include <algorithm>
+
 #include "pc_internal.cuh"
 #include "stencil_common.cuh"
 
@@ -186,6 +188,200 @@ __global__ void __launch_bounds__(256) split_e2(FieldArgs<T> a, CpmlArgs<T> p, A
     if (!isfinite(chk)) atomicOr(a.status, PC_STATUS_NONFINITE);
 }
 
+// The pole terms of the ADE E update on the fused schedule.  The fused H + E
+// kernel stored the partial value ce E^n + inv (dt/eps0) curl (ade_partial) at
+// every point of the dispersive regions in the output set; this pass subtracts
+// the poles' terms, advances the auxiliaries and stores E^{n+1}, reading E^n from
+// the input set.  Same update ranges per component as split_e3 and the same
+// arithmetic as ade_poles; a point in several boxes belongs to the first
+// (ade_region_of).  Every load of a point is issued before the first store, so a
+// thread keeps up to 3 x (2 + 2 PC_MAX_ADE_POLES) loads in flight (the stores to
+// the auxiliaries could alias later loads if they were interleaved).
+template <typename T>
+__global__ void __launch_bounds__(256) ade_pass3(FieldArgs<T> a, AdeArgs<T> A, int r) {
+    const int* b = A.box[r];
+    const int k = b[4] + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = b[2] + blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = b[0] + blockIdx.z;
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    if (k >= b[5] || j >= b[3] || i >= b[1] || k >= nz || j >= ny || i >= nx) return;
+    if (ade_region_of(A, i, j, k) != r) return;
+    const int64_t o = ((int64_t)i * ny + j) * a.pitch + k;
+    const int64_t ao = ade_offset(A, r, i, j, k);
+    const bool upd[3] = {j < ny - 1 && k < nz - 1, i < nx - 1 && k < nz - 1, i < nx - 1 && j < ny - 1};
+    const int np = A.npoles[r];
+    T e0[3], acc[3], x0[3][PC_MAX_ADE_POLES], x1[3][PC_MAX_ADE_POLES];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        e0[c] = acc[c] = T(0);
+#pragma unroll
+        for (int p = 0; p < PC_MAX_ADE_POLES; ++p) x0[c][p] = x1[c][p] = T(0);
+        if (!upd[c]) continue;
+        e0[c] = a.Ein[c][o];
+        acc[c] = a.Eout[c][o];
+#pragma unroll
+        for (int p = 0; p < PC_MAX_ADE_POLES; ++p) {
+            if (p >= np) break;
+            x0[c][p] = A.aux[r][c][p][0][ao];
+            if (A.kind[r][p] == 0) x1[c][p] = A.aux[r][c][p][1][ao];
+        }
+    }
+    const T inv = A.inv[r];
+    T chk = T(0);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (!upd[c]) continue;
+        T e = acc[c];
+#pragma unroll
+        for (int p = 0; p < PC_MAX_ADE_POLES; ++p) {
+            if (p >= np) break;
+            if (A.kind[r][p] == 0)
+                e -= inv * (A.c2[r][p] * x0[c][p] - A.c3[r][p] * x1[c][p]);
+            else if (A.kind[r][p] == 1)
+                e -= inv * (T(0.5) * A.dt * (T(1) + A.c1[r][p]) * x0[c][p]);
+            else
+                e -= inv * ((A.c1[r][p] - T(1)) * x0[c][p]);
+        }
+#pragma unroll
+        for (int p = 0; p < PC_MAX_ADE_POLES; ++p) {
+            if (p >= np) break;
+            if (A.kind[r][p] == 0) {
+                const T dn = (A.c0[r][p] * e + A.c1[r][p] * e0[c]) + (A.c2[r][p] * x0[c][p] - A.c3[r][p] * x1[c][p]);
+                A.aux[r][c][p][1][ao] = dn;
+                A.aux[r][c][p][0][ao] = x0[c][p] + dn;
+            } else {
+                A.aux[r][c][p][0][ao] = A.c1[r][p] * x0[c][p] + A.c0[r][p] * (T(0.5) * (e + e0[c]));
+            }
+        }
+        a.Eout[c][o] = e;
+        chk += e;
+    }
+    if (!isfinite(chk)) atomicOr(a.status, PC_STATUS_NONFINITE);
+}
+
+// ade_pass3 with V consecutive k points per thread (float2 accesses for V = 2):
+// for a single region whose k range starts and ends on multiples of V and ends
+// before the last k (so every component's update range is uniform over the V
+// points, and region ownership needs no per-point test).  Same arithmetic.
+template <typename T, int V>
+struct VecOf;
+template <>
+struct VecOf<float, 2> {
+    using type = float2;
+};
+
+template <typename T, int V>
+__global__ void __launch_bounds__(256) ade_pass3v(FieldArgs<T> a, AdeArgs<T> A) {
+    using VT = typename VecOf<T, V>::type;
+    const int* b = A.box[0];
+    const int k = b[4] + (int)(blockIdx.x * blockDim.x + threadIdx.x) * V;
+    const int j = b[2] + blockIdx.y * blockDim.y + threadIdx.y;
+    const int i = b[0] + blockIdx.z;
+    const int nx = a.nx, ny = a.ny;
+    if (k >= b[5] || j >= b[3] || i >= b[1] || j >= ny || i >= nx) return;
+    const int64_t o = ((int64_t)i * ny + j) * a.pitch + k;
+    const int64_t ao = ade_offset(A, 0, i, j, k);
+    const bool upd[3] = {j < ny - 1, i < nx - 1, i < nx - 1 && j < ny - 1};
+    const int np = A.npoles[0];
+    T e0[3][V], acc[3][V], x0[3][PC_MAX_ADE_POLES][V], x1[3][PC_MAX_ADE_POLES][V];
+    auto ld = [&](const T* p, T* v) {
+        const VT w = *reinterpret_cast<const VT*>(p);
+        const T* q = reinterpret_cast<const T*>(&w);
+#pragma unroll
+        for (int l = 0; l < V; ++l) v[l] = q[l];
+    };
+    auto st = [&](T* p, const T* v) {
+        VT w;
+        T* q = reinterpret_cast<T*>(&w);
+#pragma unroll
+        for (int l = 0; l < V; ++l) q[l] = v[l];
+        *reinterpret_cast<VT*>(p) = w;
+    };
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (!upd[c]) continue;
+        ld(a.Ein[c] + o, e0[c]);
+        ld(a.Eout[c] + o, acc[c]);
+#pragma unroll
+        for (int p = 0; p < PC_MAX_ADE_POLES; ++p) {
+            if (p >= np) break;
+            ld(A.aux[0][c][p][0] + ao, x0[c][p]);
+            if (A.kind[0][p] == 0) ld(A.aux[0][c][p][1] + ao, x1[c][p]);
+        }
+    }
+    const T inv = A.inv[0];
+    T chk = T(0);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (!upd[c]) continue;
+        T e[V];
+#pragma unroll
+        for (int l = 0; l < V; ++l) {
+            T v = acc[c][l];
+#pragma unroll
+            for (int p = 0; p < PC_MAX_ADE_POLES; ++p) {
+                if (p >= np) break;
+                if (A.kind[0][p] == 0)
+                    v -= inv * (A.c2[0][p] * x0[c][p][l] - A.c3[0][p] * x1[c][p][l]);
+                else if (A.kind[0][p] == 1)
+                    v -= inv * (T(0.5) * A.dt * (T(1) + A.c1[0][p]) * x0[c][p][l]);
+                else
+                    v -= inv * ((A.c1[0][p] - T(1)) * x0[c][p][l]);
+            }
+            e[l] = v;
+            chk += v;
+        }
+#pragma unroll
+        for (int p = 0; p < PC_MAX_ADE_POLES; ++p) {
+            if (p >= np) break;
+            T n0[V], n1[V];
+#pragma unroll
+            for (int l = 0; l < V; ++l) {
+                if (A.kind[0][p] == 0) {
+                    n1[l] = (A.c0[0][p] * e[l] + A.c1[0][p] * e0[c][l]) +
+                            (A.c2[0][p] * x0[c][p][l] - A.c3[0][p] * x1[c][p][l]);
+                    n0[l] = x0[c][p][l] + n1[l];
+                } else {
+                    n0[l] = A.c1[0][p] * x0[c][p][l] + A.c0[0][p] * (T(0.5) * (e[l] + e0[c][l]));
+                }
+            }
+            if (A.kind[0][p] == 0) st(A.aux[0][c][p][1] + ao, n1);
+            st(A.aux[0][c][p][0] + ao, n0);
+        }
+        st(a.Eout[c] + o, e);
+    }
+    if (!isfinite(chk)) atomicOr(a.status, PC_STATUS_NONFINITE);
+}
+
+template <typename T>
+int ade_pass_t(pc_ctx* c, int in, int out, cudaStream_t s) {
+    FieldArgs<T> a = make_field_args<T>(c, in, out);
+    AdeArgs<T> ade = make_ade_args<T>(c);
+    for (int r = 0; r < ade.nreg; ++r) {
+        const int* b = ade.box[r];
+        const int nxb = std::min(b[1], c->g.nx) - b[0], nyb = std::min(b[3], c->g.ny) - b[2];
+        const int nzb = std::min(b[5], c->g.nz) - b[4];
+        if (nxb <= 0 || nyb <= 0 || nzb <= 0) continue;
+        dim3 blk(32, 8);
+        bool vec = false;
+        if constexpr (sizeof(T) == 4) {
+            // the region's arrays and every field row are 8-byte aligned at even k - b[4]
+            const int zb = b[5] - b[4];
+            const bool single = ade.nreg == 1 && b[5] <= c->g.nz - 1;
+            // (two points per thread: 78 registers, three CTAs per SM; four points
+            // take 140 registers and one CTA per SM and run slower)
+            if (single && b[4] % 2 == 0 && zb % 2 == 0) {
+                ade_pass3v<T, 2><<<dim3((zb / 2 + 31) / 32, (nyb + 7) / 8, nxb), blk, 0, s>>>(a, ade);
+                vec = true;
+            }
+        }
+        if (!vec) ade_pass3<T><<<dim3((nzb + 31) / 32, (nyb + 7) / 8, nxb), blk, 0, s>>>(a, ade, r);
+        ++c->launches;
+    }
+    PC_CUDA_CHECK(cudaGetLastError());
+    return PC_OK;
+}
+
 template <typename T>
 int split_step_t(pc_ctx* c, cudaStream_t s, const double* tfsf_amp) {
     FieldArgs<T> a = make_field_args<T>(c, c->cur, c->cur);
@@ -238,6 +434,11 @@ int split_step_t(pc_ctx* c, cudaStream_t s, const double* tfsf_amp) {
 }
 
 }  // namespace
+
+int launch_ade_pass(pc_ctx* c, int in_set, int out_set, cudaStream_t s) {
+    if (c->g.ndim != 3) return PC_ERR_INVALID;
+    return c->g.precision == 8 ? ade_pass_t<double>(c, in_set, out_set, s) : ade_pass_t<float>(c, in_set, out_set, s);
+}
 
 int launch_split_step(pc_ctx* c, cudaStream_t s, const double* tfsf_amp) {
     return c->g.precision == 8 ? split_step_t<double>(c, s, tfsf_amp) : split_step_t<float>(c, s, tfsf_amp);

@@ -90,7 +90,44 @@ int tfsf_e_t(pc_ctx* c, double amp, cudaStream_t s) {
     return PC_OK;
 }
 
+// The auxiliary line alone, one step, for the fused schedule (which applies the
+// plane corrections inside its H + E kernel): inc[0] = e1[m0] at step n (the H
+// correction), then the H half step, inc[1] = h1[m0] at n+1/2 (the E
+// correction), then the E half step with the hard source.  The same arithmetic
+// as tfsf_h / tfsf_e; one CTA, the two half steps separated by a barrier.
+template <typename T>
+__global__ void __launch_bounds__(1024) tfsf_line(T* e1, T* h1, int M, int m0, T db_s, T cb1, T inv_dz, T amp,
+                                                  T* inc) {
+    const int t = threadIdx.x;
+    if (t == 0) inc[0] = e1[m0];
+    for (int m = t; m < M; m += blockDim.x)
+        if (m >= 1 && m <= M - 2) h1[m] -= db_s * (e1[m] - e1[m - 1]) * inv_dz;
+    __syncthreads();
+    if (t == 0) inc[1] = h1[m0];
+    for (int m = t; m < M; m += blockDim.x) {
+        if (m == 0)
+            e1[0] = amp;
+        else if (m <= M - 2)
+            e1[m] -= cb1 * (h1[m + 1] - h1[m]) * inv_dz;
+    }
+}
+
+template <typename T>
+int tfsf_line_t(pc_ctx* c, double amp, cudaStream_t s) {
+    const TfsfState& t = c->tfsf;
+    tfsf_line<T><<<1, 1024, 0, s>>>(static_cast<T*>(t.d_e1), static_cast<T*>(t.d_h1), t.M, t.m0, T(c->db_s),
+                                    T(t.cb1), T(1.0 / c->g.dz), T(amp), static_cast<T*>(t.d_inc));
+    ++c->launches;
+    PC_CUDA_CHECK(cudaGetLastError());
+    return PC_OK;
+}
+
 }  // namespace
+
+int launch_tfsf_line(pc_ctx* c, double amp, cudaStream_t s) {
+    if (!c->tfsf.on || !c->tfsf.d_inc) return PC_ERR_STATE;
+    return c->g.precision == 8 ? tfsf_line_t<double>(c, amp, s) : tfsf_line_t<float>(c, amp, s);
+}
 
 int launch_tfsf_h(pc_ctx* c, cudaStream_t s) {
     return c->g.precision == 8 ? tfsf_h_t<double>(c, s) : tfsf_h_t<float>(c, s);

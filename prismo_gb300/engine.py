@@ -562,6 +562,23 @@ class FDTDEngine:
         if self.is_2d or not self.pingpong:
             return None
         blocked = self.time_blocking_active()
+        if not blocked and (getattr(self, "ade_aux", None) or getattr(self, "tfsf", None) is not None or self.dfts
+                            or self.fluxes or self.mode_mons):
+            # ADE auxiliaries, the TFSF line and monitor sums would advance with the
+            # timed steps: time a plain engine of the same grid on the same kernels
+            # (the chunk choice does not depend on those extras' few per-point terms)
+            if self.has_ca or self.has_hcoef:
+                return None
+            shadow = FDTDEngine(self.dims, self.spacing, self.dt, is_2d=False, precision=self.precision,
+                                sched="fused", pml=self.pml, device=str(self.device), stream=self.stream)
+            try:
+                shadow.set_time_blocking(0)
+                res = shadow.autotune(candidates, steps, cache)
+            finally:
+                shadow.close()
+            if res is not None:
+                self.set_chunk(*res)
+            return res
         key = f"{self.dims}|t={0 if self.pml is None else self.pml.thickness}|{self.precision}|" \
               f"{'ts' if blocked else 'fused'}|{torch.cuda.get_device_name(self.device)}"
         path = os.environ.get("PRISMO_GB300_CACHE", os.path.join(os.path.expanduser("~"), ".cache",
@@ -665,6 +682,12 @@ class FDTDEngine:
 
     def chunk_edge(self) -> int:
         return int(self.lib.pc_get_tuning(self.ctx, _lib.PC_TUNE_FUSED_CHUNK_EDGE))
+
+    def set_fused_extras(self, on: bool = True):
+        """3D grids with ADE regions or a TFSF plane: on the fused schedule (the
+        plane corrections and the ADE partial update in the fused H + E kernel, the
+        pole terms in one pass per region; default) or on the split kernels."""
+        _lib.check(self.lib.pc_set_tuning(self.ctx, _lib.PC_TUNE_FUSED_EXTRAS, int(bool(on))), "pc_set_tuning")
 
     def set_graph_steps(self, n: int):
         """Steps per captured time-loop graph (a multiple of 16; 0 = eager steps)."""

@@ -33,8 +33,8 @@ def poles(dt):
             O.lorentz_coeffs(0.7, 5.5e15, 4.0e14, dt)]
 
 
-@pytest.mark.parametrize("is2d", [False, True])
-def test_ade_matches_oracle(torch, is2d):
+@pytest.mark.parametrize("is2d,fused", [(False, True), (False, False), (True, False)])
+def test_ade_matches_oracle(torch, is2d, fused):
     from prismo_gb300.engine import FDTDEngine
     from prismo_gb300.pml import PMLParams
 
@@ -63,6 +63,7 @@ def test_ade_matches_oracle(torch, is2d):
         eng = FDTDEngine(g.dims, g.spacing, dt, is_2d=is2d, precision=prec, material_arrays={"eps_rel": eps},
                          pml=PMLParams(thickness=4))
         eng.set_dispersive([(box, 1.0, pl)])
+        eng.set_fused_extras(fused)
         eng.add_source(comp, eng.offsets(comp, src), None, wf)
         t = np.cumsum(np.full(n, dt))
         eng.step(n, np.array([wf(x) for x in t])[:, None])

@@ -175,7 +175,7 @@ def test_dispersive_384_fp32_vs_fp64_full_length(torch):
     for g, e in to_peak.items():
         assert e <= 1e-5, (g, e)
     for q, m in enumerate(info["dft_ids"]):
-        a, b = e32.dft_result(m).double(), e64.dft_result(m).double()
+        a, b = e32.dft_result(m).to(torch.complex128), e64.dft_result(m).to(torch.complex128)
         e = ((a - b).reshape(a.shape[0], -1).norm(dim=1) / b.reshape(b.shape[0], -1).norm(dim=1)).max().item()
         print(f"DFT plane {q}: max per-frequency rel L2 {e:.2e}")
         assert e <= 1e-4, (q, e)

@@ -26,8 +26,9 @@ def rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
+@pytest.mark.parametrize("fused", [True, False])
 @pytest.mark.parametrize("direction,pol", [(-1, "x"), (1, "y")])
-def test_tfsf_matches_oracle(torch, direction, pol):
+def test_tfsf_matches_oracle(torch, direction, pol, fused):
     from prismo_gb300.engine import FDTDEngine
     from prismo_gb300.pml import PMLParams
 
@@ -45,6 +46,7 @@ def test_tfsf_matches_oracle(torch, direction, pol):
         eng = FDTDEngine(g.dims, g.spacing, dt, is_2d=False, precision=prec, material_arrays={"eps_rel": eps},
                          pml=PMLParams(thickness=4))
         eng.set_tfsf(k0, direction, pol, wf)
+        eng.set_fused_extras(fused)
         t = np.cumsum(np.full(n, dt))
         eng.step(n, np.array([wf(x) for x in t])[:, None])
         assert eng.check_status() == 0
