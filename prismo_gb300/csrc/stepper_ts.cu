@@ -388,46 +388,25 @@ __device__ __forceinline__ void e_pair(const TsArgs& A, const TsPc* pc, const Ts
                       u[5]);
 }
 
-// Region row r and pair column u of thread `tid` (< RJ * NPR).  With z CPML in
-// the variant, the pair columns holding z-slab points come first, so that warps
-// hold either slab pairs or none and only the former run the z recursions.
-template <int K, int AX>
-__device__ __forceinline__ void pair_of(int tid, int k0, int nz, int t, int& r, int& u) {
-    constexpr int NPR = TsGeom<K>::NPR;
-    auto slab_pair = [&](int v) {
-        const int k = k0 - 2 + 2 * v;
-        const bool s0 = k >= 0 && k < nz && (k < t || k >= nz - t);
-        const bool s1 = k + 1 >= 0 && k + 1 < nz && (k + 1 < t || k + 1 >= nz - t);
-        return s0 || s1;
-    };
-    int ns = 0;
-    if (AX & 4)
-        for (int v = 0; v < NPR; ++v) ns += slab_pair(v) ? 1 : 0;
-    if (ns == 0 || ns == NPR) {
-        r = tid / NPR;
-        u = tid - r * NPR;
-        return;
-    }
-    const int rows_slab = TsGeom<K>::RJ * ns;
-    const bool want_slab = tid < rows_slab;
-    int want;
-    if (want_slab) {
-        r = tid / ns;
-        want = tid - r * ns;
+// Region row r and pair column u of thread `tid` (< RJ * NPR).  Each half-warp
+// takes the 16 inner pair columns (u = 1..16, 32 consecutive floats) of one row,
+// so its float2 shared-memory accesses touch 32 distinct banks; the two outer
+// columns of every row (u = 0, NPR - 1) follow, two per thread pair.  (A plain
+// row-major order puts 18 pairs in a row: half-warps straddling two rows then
+// hit the same banks twice.  Packing the z-slab pairs of a CPML item first, so
+// that fewer warps run the z recursions, measured slower than this order: 85.0
+// against 88.0 Gcell/s at 256^3.)
+template <int K>
+__device__ __forceinline__ void pair_of(int tid, int& r, int& u) {
+    constexpr int NPR = TsGeom<K>::NPR, RJ = TsGeom<K>::RJ, NM = NPR - 2;
+    static_assert(NM == 16, "a half-warp spans the inner pair columns of a row");
+    if (tid < RJ * NM) {
+        r = tid / NM;
+        u = 1 + (tid - r * NM);
     } else {
-        const int v2 = tid - rows_slab, nn = NPR - ns;
-        r = v2 / nn;
-        want = v2 - r * nn;
-    }
-    u = 0;
-    for (int v = 0, seen = 0; v < NPR; ++v) {
-        if (slab_pair(v) == want_slab) {
-            if (seen == want) {
-                u = v;
-                break;
-            }
-            ++seen;
-        }
+        const int v = tid - RJ * NM;
+        r = v >> 1;
+        u = (v & 1) ? NPR - 1 : 0;
     }
 }
 
@@ -481,7 +460,7 @@ __device__ __forceinline__ void ts3_item(const TsArgs& A, const TsMaps& maps, co
     // ---- this thread's pair of region points ----------------------------------
     const bool act = tid < G::NPAIR;
     int r = 0, u = 0;
-    if (act) pair_of<K, AX>(tid, k0, nz, t, r, u);
+    if (act) pair_of<K>(tid, r, u);
     const int si = r * TS_BW + 2 * u + G::CO;  // even: float2 accesses stay aligned
     const int j = j0 - K + r;
     const int kp = k0 - 2 + 2 * u;  // the pair's first k (even when k0 is)
@@ -551,7 +530,7 @@ __device__ __forceinline__ void ts3_item(const TsArgs& A, const TsMaps& maps, co
     }
     if (CP && !psi_ok) atomicOr(A.status, PC_STATUS_BOUNDS);  // psi traffic of this pair is skipped
     // psi work only where this pair or the plane lies in a slab (warp-uniform for
-    // the x slabs, and mostly so for y and z with the pair order of pair_of)
+    // the x slabs)
     const bool yzs = CP && psi_ok &&
                      (((AX & 2) && rw.sy >= 0 && (pc[0].kjd || pc[1].kjd)) || ((AX & 4) && (pc[0].sz >= 0 || pc[1].sz >= 0)));
     auto use_psi = [&](const TsPlane& P) { return CP && psi_ok && (yzs || P.sx >= 0); };
