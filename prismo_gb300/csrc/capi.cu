@@ -40,6 +40,7 @@ int dft_monitor_init(DftMonitor& m, int comp, const int64_t* offsets, int npts, 
     for (int i = 0; i < npts; ++i)
         if (offsets[i] < 0 || offsets[i] >= limit) return PC_ERR_INVALID;
     m = DftMonitor{};
+    m.plane_k = -1;
     m.comp = comp;
     m.npts = npts;
     m.nf = nf;
@@ -360,6 +361,7 @@ int advance(pc_ctx* c, int n, int left, const double* tamp, cudaStream_t s) {
         // ADE / TFSF on the fused schedule: the TFSF line first (incident values of
         // this step), the fused H + E pass (ADE points get the partial update), then
         // the ADE pole terms on the new set
+        plan_fused_dft(c);  // plane DFT samples written by the kernels below
         rc = c->tfsf.on ? launch_tfsf_line(c, *tamp, s) : PC_OK;
         if (!rc) rc = launch_fused_step(c, s, tamp);
         if (!rc && c->ade_n > 0) rc = launch_ade_pass(c, c->cur ^ 1, c->cur, s);
@@ -520,6 +522,23 @@ int pc_add_dft(pc_ctx* c, int32_t comp, const int64_t* offsets, int32_t npts, co
     const int rc = dft_monitor_init(m, comp, offsets, npts, omega, nf, dt, t0, d_acc,
                                     (int64_t)c->g.nx * c->g.ny * c->g.pitch);
     if (rc) return rc;
+    m.plane_k = -1;
+    if (c->g.ndim == 3 && comp < 3 && offsets[0] >= 0 && offsets[0] < c->g.nz) {
+        // a whole z-plane in (i, j) order?
+        const int64_t P = c->g.pitch, k = offsets[0];
+        int ny = 1;
+        while (ny < npts && offsets[ny] == offsets[ny - 1] + P) ++ny;
+        const int nx = npts / ny;
+        bool plane = ny <= c->g.ny && nx <= c->g.nx && (int64_t)nx * ny == npts;
+        for (int i = 0; plane && i < nx; ++i)
+            for (int j = 0; plane && j < ny; ++j)
+                plane = offsets[(int64_t)i * ny + j] == ((int64_t)i * c->g.ny + j) * P + k;
+        if (plane) {
+            m.plane_k = (int)k;
+            m.plane_nx = nx;
+            m.plane_ny = ny;
+        }
+    }
     c->dfts.push_back(m);
     return (int)c->dfts.size() - 1;
 }

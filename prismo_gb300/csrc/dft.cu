@@ -89,6 +89,14 @@ int launch_dft_flush_rows(DftMonitor& m, int rows, cudaStream_t s) {
 
 int dft_after_step(pc_ctx* c, cudaStream_t s) {
     for (auto& m : c->dfts) {
+        if (m.fused) {  // the stepping kernels wrote ring row m.rows
+            m.fused = false;
+            if (++m.rows == m.T) {
+                const int rc = dft_flush_monitor(c, m, s);
+                if (rc) return rc;
+            }
+            continue;
+        }
         const int threads = 256;
         const int blocks = (m.npts + threads - 1) / threads < 1024 ? (m.npts + threads - 1) / threads : 1024;
         if (c->g.precision == 8)

@@ -40,6 +40,21 @@ struct DftMonitor {
     double2* d_state; // [nf] float64 phase of the next sample (ctx-owned)
     double2* d_rot;   // [nf] exp(-i w dt) (ctx-owned)
     float4* d_acc;    // [nf][npts] (sum re, sum im, comp re, comp im), caller-owned
+    // a whole z-plane of an E component: point i * plane_ny + j is cell (i, j, plane_k)
+    // for i < plane_nx, j < plane_ny (plane_k = -1: any other point set)
+    int plane_k, plane_nx, plane_ny;
+    bool fused;       // sampled by the stepping kernels this step (no dft_sample launch)
+    int fused_where;  // 1: by the fused H + E kernel, 2: by the ADE pole pass
+};
+
+// Plane DFT monitors whose samples a stepping kernel writes into the ring row of
+// the current step (see plan_fused_dft).
+#define PC_MAX_FUSED_DFT 2
+template <typename T>
+struct KernelDft {
+    int n;
+    int comp[PC_MAX_FUSED_DFT], k[PC_MAX_FUSED_DFT], nx[PC_MAX_FUSED_DFT], ny[PC_MAX_FUSED_DFT];
+    float* row[PC_MAX_FUSED_DFT];
 };
 
 // Flux plane: per step, sum over its points of (F0 F1 - F2 F3) times `scale`
@@ -225,6 +240,12 @@ int launch_fused_step(pc_ctx* c, cudaStream_t s, const double* tfsf_amp = nullpt
 // The fused schedule with ADE regions and / or a TFSF plane: the stepper needs a
 // TFSF plane (if any) clear of the ADE boxes' k ranges.
 bool fused_extras_ok(const pc_ctx* c);
+// Marks the plane DFT monitors that the fused kernel (planes outside the ADE
+// boxes) or the ADE pole pass (planes inside the single ADE box) sample this step;
+// only without soft sources, which are added after those kernels.
+void plan_fused_dft(pc_ctx* c);
+template <typename T>
+KernelDft<T> kernel_dft(const pc_ctx* c, int where);
 int launch_tfsf_line(pc_ctx* c, double amp, cudaStream_t s);
 int launch_ade_pass(pc_ctx* c, int in_set, int out_set, cudaStream_t s);
 void destroy_fused_state(pc_ctx* c);
@@ -233,7 +254,7 @@ bool ts_eligible(const pc_ctx* c);
 bool ts_two_step_ok(pc_ctx* c);
 int launch_ts_step(pc_ctx* c, int k, int row, cudaStream_t s, bool* fused_sources);
 void destroy_ts_state(pc_ctx* c);
-int dft_after_step(pc_ctx* c, cudaStream_t s);
+int dft_after_step(pc_ctx* c, cudaStream_t s);  // skips the monitors marked fused
 int launch_dft_sample_f32(const float* field, DftMonitor& m, int row, cudaStream_t s);
 int launch_dft_flush_rows(DftMonitor& m, int rows, cudaStream_t s);
 int dft_monitor_init(DftMonitor& m, int comp, const int64_t* offsets, int npts, const double* omega, int nf, double dt,

@@ -36,11 +36,12 @@ struct FusedMaps {
     CUtensorMap cb[3];  // Cb of the E update, staged with the fields
 };
 
-// Work the fused kernel does for dispersive regions and a TFSF plane (all zero:
-// none).  E points inside an ADE box get the partial update ade_partial (the
-// pole terms follow in ade_pass3); the TFSF plane corrections of tfsf.cu are
-// added to H at k = tf_kH and to E at k = tf_k0, from the incident values that
-// tfsf_line wrote for this step.
+// Work the fused kernel does for dispersive regions, a TFSF plane and plane DFT
+// monitors (all zero: none).  E points inside an ADE box get the partial update
+// ade_partial (the pole terms follow in ade_pass3); the TFSF plane corrections of
+// tfsf.cu are added to H at k = tf_kH and to E at k = tf_k0, from the incident
+// values that tfsf_line wrote for this step; the final E of a monitored plane
+// point is written to its monitor's ring row (what dft_sample would copy).
 template <typename T>
 struct FusedXtra {
     int nbox;
@@ -50,11 +51,15 @@ struct FusedXtra {
     int tf_on, tf_kH, tf_k0, tf_pol;  // pol 0: Hy at kH and Ex at k0; 1: Hx and Ey
     T tf_sgn;
     const T* tf_inc;  // [2]: incident E at step n, incident H at n+1/2
+    KernelDft<T> dft;  // plane DFT monitors sampled from the E epilogue
 };
 
 namespace {
 
 constexpr uint32_t kWaitLimit = 1u << 22;
+// plane DFT monitors the fused kernel samples (one: a second one spills registers
+// of the E epilogue; further planes keep their dft_sample launch)
+constexpr int kFusedDft = 1;
 
 // Tile geometry: a CTA updates a TY x TZ tile of (j, k) for every plane of its
 // x-chunk.  Eight consumer warps own the tile (lane = k, RPT rows per thread);
@@ -106,7 +111,7 @@ enum { CL_PLAIN, CL_GEN, CL_YZ, CL_XZ, CL_XY, CL_Z, CL_Y, CL_X, CL_N };
 // warp + TY/2 of the tile.  AX: the CPML axes this variant handles (bit 0 x, bit 1
 // y, bit 2 z; 0 = no CPML code); the host gives a variant only items whose planes
 // and tile (with halo) stay clear of the slabs of the other axes.
-template <typename T, int TY, int TZ, int S, int AX, bool HCOEF, bool CA>
+template <typename T, int TY, int TZ, int S, int AX, bool HCOEF, bool CA, bool DFT = false>
 __device__ __forceinline__ void fused3_item(const FieldArgs<T>& a, const CpmlArgs<T>& pm, const int4 item,
                                             const FusedMaps& maps, const FusedXtra<T>& xt) {
     using G = FusedGeom<T, TY, TZ>;
@@ -139,18 +144,28 @@ __device__ __forceinline__ void fused3_item(const FieldArgs<T>& a, const CpmlArg
     const T idx_ = a.inv_dx, idy = a.inv_dy, idz = a.inv_dz;
     // dispersive regions this item's E planes [ib, ie) and tile reach; TFSF values
     // (the region loops are unrolled so that xt is indexed statically: a dynamic
-    // index into a kernel parameter would copy it to local memory)
+    // index into a kernel parameter would copy it to local memory).  XT: the
+    // variants that compile this work (not the float32 ones with per-cell H or Ca
+    // coefficients, whose registers it would spill; such grids step on the split
+    // kernels when they have ADE regions or a TFSF plane, fused_extras_ok).
+    constexpr bool XT = sizeof(T) == 8 || (!HCOEF && !CA);
     bool ade_cta = false;
 #pragma unroll
     for (int r = 0; r < PC_MAX_ADE_REGIONS; ++r) {
         const int* b = xt.box[r];
-        ade_cta = ade_cta || (r < xt.nbox && ib < b[1] && ie > b[0] && j0 < b[3] && j0 + TY > b[2] && k0 < b[5] &&
-                              k0 + TZ > b[4]);
+        ade_cta = ade_cta || (XT && r < xt.nbox && ib < b[1] && ie > b[0] && j0 < b[3] && j0 + TY > b[2] &&
+                              k0 < b[5] && k0 + TZ > b[4]);
     }
-    const bool tf_h = xt.tf_on && xt.tf_kH >= k0 && xt.tf_kH <= k0 + TZ;  // incl. the helper's halo column
-    const bool tf_e = xt.tf_on && xt.tf_k0 >= k0 && xt.tf_k0 < k0 + TZ;
+    const bool tf_h = XT && xt.tf_on && xt.tf_kH >= k0 && xt.tf_kH <= k0 + TZ;  // incl. the helper's halo column
+    const bool tf_e = XT && xt.tf_on && xt.tf_k0 >= k0 && xt.tf_k0 < k0 + TZ;
     const T inc_h = tf_h ? xt.tf_inc[0] : T(0);
     const T inc_e = tf_e ? xt.tf_inc[1] : T(0);
+    bool dft_cta = false;  // a monitored plane crosses this tile (DFT: the instantiation that samples)
+    if (DFT) {
+#pragma unroll
+        for (int m = 0; m < kFusedDft; ++m)
+            dft_cta = dft_cta || (m < xt.dft.n && xt.dft.k[m] >= k0 && xt.dft.k[m] < k0 + TZ);
+    }
 
     if (helper && lane == 0) {
         for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
@@ -521,6 +536,14 @@ __device__ __forceinline__ void fused3_item(const FieldArgs<T>& a, const CpmlArg
                             if (q <= nx - 2) ey += cb1 * inc_e * idz;
                         }
                     }
+                    if (DFT && dft_cta) {
+#pragma unroll
+                        for (int m = 0; m < kFusedDft; ++m)
+                            if (m < xt.dft.n && k == xt.dft.k[m] && q < xt.dft.nx[m] && j < xt.dft.ny[m]) {
+                                const T v = xt.dft.comp[m] == 0 ? ex : (xt.dft.comp[m] == 1 ? ey : ez);
+                                xt.dft.row[m][(int64_t)q * xt.dft.ny[m] + j] = static_cast<float>(v);
+                            }
+                    }
                     a.Eout[0][o] = ex;
                     a.Eout[1][o] = ey;
                     a.Eout[2][o] = ez;
@@ -561,7 +584,9 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
 
 // Every class in one launch (float32, no per-cell H or Ca coefficients): the class
 // of an item sits in the top byte of its w; the CTA runs that class's variant.
-template <typename T, int TY, int TZ, int S>
+// DFT: the instantiation that writes plane DFT samples from the E epilogue (only
+// launched when a monitor is sampled here, so the common one keeps its registers).
+template <typename T, int TY, int TZ, int S, bool DFT>
 __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
     fused3_multi(FieldArgs<T> a, CpmlArgs<T> pm, const int4* __restrict__ items,
                  const __grid_constant__ FusedMaps maps, const FusedXtra<T> xt) {
@@ -569,14 +594,14 @@ __global__ void __launch_bounds__(TZ*(TY / 2 + 1), (sizeof(T) == 4 ? 2 : 1))
     const int cls = it.w >> 24;
     it.w &= 0xFFFFFF;
     switch (cls) {
-        case CL_PLAIN: fused3_item<T, TY, TZ, S, 0, false, false>(a, pm, it, maps, xt); break;
-        case CL_Z: fused3_item<T, TY, TZ, S, 4, false, false>(a, pm, it, maps, xt); break;
-        case CL_Y: fused3_item<T, TY, TZ, S, 2, false, false>(a, pm, it, maps, xt); break;
-        case CL_X: fused3_item<T, TY, TZ, S, 1, false, false>(a, pm, it, maps, xt); break;
-        case CL_YZ: fused3_item<T, TY, TZ, S, 6, false, false>(a, pm, it, maps, xt); break;
-        case CL_XZ: fused3_item<T, TY, TZ, S, 5, false, false>(a, pm, it, maps, xt); break;
-        case CL_XY: fused3_item<T, TY, TZ, S, 3, false, false>(a, pm, it, maps, xt); break;
-        default: fused3_item<T, TY, TZ, S, 7, false, false>(a, pm, it, maps, xt); break;
+        case CL_PLAIN: fused3_item<T, TY, TZ, S, 0, false, false, DFT>(a, pm, it, maps, xt); break;
+        case CL_Z: fused3_item<T, TY, TZ, S, 4, false, false, DFT>(a, pm, it, maps, xt); break;
+        case CL_Y: fused3_item<T, TY, TZ, S, 2, false, false, DFT>(a, pm, it, maps, xt); break;
+        case CL_X: fused3_item<T, TY, TZ, S, 1, false, false, DFT>(a, pm, it, maps, xt); break;
+        case CL_YZ: fused3_item<T, TY, TZ, S, 6, false, false, DFT>(a, pm, it, maps, xt); break;
+        case CL_XZ: fused3_item<T, TY, TZ, S, 5, false, false, DFT>(a, pm, it, maps, xt); break;
+        case CL_XY: fused3_item<T, TY, TZ, S, 3, false, false, DFT>(a, pm, it, maps, xt); break;
+        default: fused3_item<T, TY, TZ, S, 7, false, false, DFT>(a, pm, it, maps, xt); break;
     }
 }
 
@@ -743,9 +768,69 @@ int choose_chunk(const pc_grid_desc& g, int smem) {
     return cx;
 }
 
+}  // namespace
+
+// fused_t runs every item class in one fused3_multi launch (the one launch that
+// can sample DFT planes): float32, no per-cell H or Ca coefficients, CPML
+static bool fused_unified_path(const pc_ctx* c) {
+    return c->g.precision == 4 && !c->ca[0] && !c->da[0] && c->fused_split > 0 && c->fused_unified != 0 &&
+           c->cpml_t > 0;
+}
+
+void plan_fused_dft(pc_ctx* c) {
+    int n[3] = {0, 0, 0};
+    const pc_grid_desc& g = c->g;
+    const bool unified = fused_unified_path(c);
+    for (auto& m : c->dfts) {
+        m.fused = false;
+        m.fused_where = 0;
+        if (m.plane_k < 0 || m.comp > 2 || !c->sources.empty() || g.ndim != 3) continue;
+        const int k = m.plane_k;
+        bool in_box = false;
+        for (int r = 0; r < c->ade_n; ++r) in_box = in_box || (k >= c->ade[r].box[4] && k < c->ade[r].box[5]);
+        int where = 0;
+        if (!in_box) {
+            where = unified ? 1 : 0;
+        } else if (c->ade_n == 1) {
+            // the whole plane inside the box and inside the component's update range
+            const int* b = c->ade[0].box;
+            const bool inside = b[0] <= 0 && m.plane_nx <= b[1] && b[2] <= 0 && m.plane_ny <= b[3];
+            const bool upd = m.comp == 0   ? (m.plane_ny <= g.ny - 1 && k <= g.nz - 2)
+                             : m.comp == 1 ? (m.plane_nx <= g.nx - 1 && k <= g.nz - 2)
+                                           : (m.plane_nx <= g.nx - 1 && m.plane_ny <= g.ny - 1);
+            if (inside && upd) where = 2;
+        }
+        if (where && n[where] < (where == 1 ? kFusedDft : PC_MAX_FUSED_DFT)) {
+            ++n[where];
+            m.fused = true;
+            m.fused_where = where;
+        }
+    }
+}
+
+template <typename T>
+KernelDft<T> kernel_dft(const pc_ctx* c, int where) {
+    KernelDft<T> d{};
+    for (const auto& m : c->dfts) {
+        if (!m.fused || m.fused_where != where || d.n >= PC_MAX_FUSED_DFT) continue;
+        d.comp[d.n] = m.comp;
+        d.k[d.n] = m.plane_k;
+        d.nx[d.n] = m.plane_nx;
+        d.ny[d.n] = m.plane_ny;
+        d.row[d.n] = m.d_ring + (size_t)m.rows * m.npts;
+        ++d.n;
+    }
+    return d;
+}
+template KernelDft<float> kernel_dft<float>(const pc_ctx*, int);
+template KernelDft<double> kernel_dft<double>(const pc_ctx*, int);
+
+namespace {
+
 template <typename T>
 FusedXtra<T> make_fused_xtra(const pc_ctx* c, bool tfsf) {
     FusedXtra<T> x{};
+    x.dft = kernel_dft<T>(c, 1);
     x.nbox = c->ade_n;
     for (int r = 0; r < c->ade_n; ++r) {
         for (int q = 0; q < 6; ++q) x.box[r][q] = c->ade[r].box[q];
@@ -870,13 +955,17 @@ int fused_t(pc_ctx* c, cudaStream_t s, bool tfsf) {
                 if constexpr (sizeof(T) == 4) {
                     static bool attr = false;
                     if (!attr) {
-                        PC_CUDA_CHECK(cudaFuncSetAttribute(fused3_multi<T, TY, TZ, S>,
-                                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                           fused_smem_bytes<T, TY, TZ, S>() +
-                                                               9 * 2 * PC_MAX_CPML * (int)sizeof(T)));
+                        const int smax = fused_smem_bytes<T, TY, TZ, S>() + 9 * 2 * PC_MAX_CPML * (int)sizeof(T);
+                        PC_CUDA_CHECK(cudaFuncSetAttribute(fused3_multi<T, TY, TZ, S, false>,
+                                                           cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
+                        PC_CUDA_CHECK(cudaFuncSetAttribute(fused3_multi<T, TY, TZ, S, true>,
+                                                           cudaFuncAttributeMaxDynamicSharedMemorySize, smax));
                         attr = true;
                     }
-                    fused3_multi<T, TY, TZ, S><<<n, dim3(TZ, TY / 2 + 1), smem, sq>>>(a, p, it, m, xt);
+                    if (xt.dft.n > 0)
+                        fused3_multi<T, TY, TZ, S, true><<<n, dim3(TZ, TY / 2 + 1), smem, sq>>>(a, p, it, m, xt);
+                    else
+                        fused3_multi<T, TY, TZ, S, false><<<n, dim3(TZ, TY / 2 + 1), smem, sq>>>(a, p, it, m, xt);
                     PC_CUDA_CHECK(cudaGetLastError());
                 }
             } else if (q == CL_GEN) {
@@ -1071,6 +1160,7 @@ extern "C" int pc_fused_steps_noalloc(const pc_grid_desc* d, void* const set0[6]
 bool fused_extras_ok(const pc_ctx* c) {
     const pc_grid_desc& g = c->g;
     if (g.ndim != 3 || g.mode != PC_MODE_CORRECTED || !c->F[1][0]) return false;
+    if (g.precision == 4 && (c->ca[0] || c->da[0])) return false;  // those variants leave the extras out
     if (c->cpml_t > 0 && psi_layout(g, c->cpml_t).total >= ((int64_t)1 << 31)) return false;
     if (c->tfsf.on) {
         if (!c->tfsf.d_inc) return false;

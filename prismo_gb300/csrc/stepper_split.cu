@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(256) split_e2(FieldArgs<T> a, CpmlArgs<T> p, A
 // thread keeps up to 3 x (2 + 2 PC_MAX_ADE_POLES) loads in flight (the stores to
 // the auxiliaries could alias later loads if they were interleaved).
 template <typename T>
-__global__ void __launch_bounds__(256) ade_pass3(FieldArgs<T> a, AdeArgs<T> A, int r) {
+__global__ void __launch_bounds__(256) ade_pass3(FieldArgs<T> a, AdeArgs<T> A, int r, KernelDft<T> D) {
     const int* b = A.box[r];
     const int k = b[4] + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = b[2] + blockIdx.y * blockDim.y + threadIdx.y;
@@ -255,6 +255,10 @@ __global__ void __launch_bounds__(256) ade_pass3(FieldArgs<T> a, AdeArgs<T> A, i
         }
         a.Eout[c][o] = e;
         chk += e;
+#pragma unroll
+        for (int m = 0; m < PC_MAX_FUSED_DFT; ++m)  // plane DFT samples of the final E
+            if (m < D.n && D.comp[m] == c && k == D.k[m] && i < D.nx[m] && j < D.ny[m])
+                D.row[m][(int64_t)i * D.ny[m] + j] = static_cast<float>(e);
     }
     if (!isfinite(chk)) atomicOr(a.status, PC_STATUS_NONFINITE);
 }
@@ -271,7 +275,7 @@ struct VecOf<float, 2> {
 };
 
 template <typename T, int V>
-__global__ void __launch_bounds__(256) ade_pass3v(FieldArgs<T> a, AdeArgs<T> A) {
+__global__ void __launch_bounds__(256) ade_pass3v(FieldArgs<T> a, AdeArgs<T> A, KernelDft<T> D) {
     using VT = typename VecOf<T, V>::type;
     const int* b = A.box[0];
     const int k = b[4] + (int)(blockIdx.x * blockDim.x + threadIdx.x) * V;
@@ -349,6 +353,13 @@ __global__ void __launch_bounds__(256) ade_pass3v(FieldArgs<T> a, AdeArgs<T> A) 
             st(A.aux[0][c][p][0] + ao, n0);
         }
         st(a.Eout[c] + o, e);
+#pragma unroll
+        for (int m = 0; m < PC_MAX_FUSED_DFT; ++m)  // plane DFT samples of the final E
+            if (m < D.n && D.comp[m] == c && i < D.nx[m] && j < D.ny[m]) {
+#pragma unroll
+                for (int l = 0; l < V; ++l)
+                    if (k + l == D.k[m]) D.row[m][(int64_t)i * D.ny[m] + j] = static_cast<float>(e[l]);
+            }
     }
     if (!isfinite(chk)) atomicOr(a.status, PC_STATUS_NONFINITE);
 }
@@ -357,6 +368,7 @@ template <typename T>
 int ade_pass_t(pc_ctx* c, int in, int out, cudaStream_t s) {
     FieldArgs<T> a = make_field_args<T>(c, in, out);
     AdeArgs<T> ade = make_ade_args<T>(c);
+    const KernelDft<T> D = kernel_dft<T>(c, 2);  // (plan_fused_dft: only with a single region)
     for (int r = 0; r < ade.nreg; ++r) {
         const int* b = ade.box[r];
         const int nxb = std::min(b[1], c->g.nx) - b[0], nyb = std::min(b[3], c->g.ny) - b[2];
@@ -371,11 +383,11 @@ int ade_pass_t(pc_ctx* c, int in, int out, cudaStream_t s) {
             // (two points per thread: 78 registers, three CTAs per SM; four points
             // take 140 registers and one CTA per SM and run slower)
             if (single && b[4] % 2 == 0 && zb % 2 == 0) {
-                ade_pass3v<T, 2><<<dim3((zb / 2 + 31) / 32, (nyb + 7) / 8, nxb), blk, 0, s>>>(a, ade);
+                ade_pass3v<T, 2><<<dim3((zb / 2 + 31) / 32, (nyb + 7) / 8, nxb), blk, 0, s>>>(a, ade, D);
                 vec = true;
             }
         }
-        if (!vec) ade_pass3<T><<<dim3((nzb + 31) / 32, (nyb + 7) / 8, nxb), blk, 0, s>>>(a, ade, r);
+        if (!vec) ade_pass3<T><<<dim3((nzb + 31) / 32, (nyb + 7) / 8, nxb), blk, 0, s>>>(a, ade, r, D);
         ++c->launches;
     }
     PC_CUDA_CHECK(cudaGetLastError());

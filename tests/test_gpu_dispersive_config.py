@@ -71,15 +71,29 @@ def test_fused_and_split_dispersive_schedules_agree(torch):
 
     dims, cpml, n = (40, 36, 64), 6, 400
     for prec, tol in (("fp64", 1e-12), ("fp32", 1e-6)):
-        out = {}
+        out, spec, per_step = {}, {}, {}
         for fused in (True, False):
             eng, info = build_dispersive_engine(dims, precision=prec, cpml=cpml, z_metal=24, ridge_width=0.3e-6)
             eng.set_fused_extras(fused)
             t = (np.arange(n) + 1) * info["dt"]
+            n0 = eng.launch_count()
             eng.step(n, info["waveform"](t)[:, None])
+            per_step[fused] = (eng.launch_count() - n0) / n
             assert eng.check_status() == 0
             out[fused] = {c: eng.component(c).double().cpu().numpy() for c in O.COMPONENTS}
+            spec[fused] = [eng.dft_result(m).cpu().numpy() for m in info["dft_ids"]]
             eng.close()
+        # the DFT planes (one above the metal, one inside it) are sampled by the
+        # fused kernel and the ADE pass on the fused schedule, by dft_sample on the
+        # split one; float32: TFSF line + fused kernel + ADE pass per step, plus the
+        # flushes every 16 steps
+        print(f"{prec}: launches per step fused {per_step[True]:.2f}, split {per_step[False]:.2f}")
+        if prec == "fp32":
+            assert per_step[True] <= 3.3, per_step
+        for q in range(len(spec[True])):
+            a, b = spec[True][q], spec[False][q]
+            e = np.linalg.norm(a - b) / np.linalg.norm(b)
+            assert e <= (1e-12 if prec == "fp64" else 1e-5), (prec, q, e)
         for c in O.COMPONENTS:
             a, b = out[True][c], out[False][c]
             if prec == "fp64":
