@@ -124,7 +124,7 @@ def config2(steps=2000, snapshots=(500, 1000)):
 
 
 # -- configuration 3: 384x384x192 dispersive, TFSF, two 64-frequency Ex planes ----------
-def config3(steps=1000, snapshots=(300, 600)):
+def config3(steps=1000, snapshots=(300, 600, 1000, 1500)):
     from prismo_gb300.materials import DrudeLorentzMaterial
     from prismo_gb300.workloads import (CONFIG_3D_DISPERSIVE, config_3d_dispersive, dispersive_monitor_planes,
                                         wavelengths_to_freqs)
