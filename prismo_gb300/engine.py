@@ -551,7 +551,7 @@ class FDTDEngine:
         candidate with CUDA events.  Fused schedule: first one length for every
         tile, then, with that fixed for the inner tiles, the length for tiles that
         touch a y or z CPML slab; returns (chunk, edge chunk).  Temporally blocked
-        stepper: the chunk length, then the work-item order; returns (chunk,
+        stepper: every pair of chunk length and work-item order; returns (chunk,
         order).  The fields and psi are restored afterwards.  Results are cached
         per (dims, CPML thickness, precision, schedule) in ``$PRISMO_GB300_CACHE``
         (default ~/.cache/prismo_gb300/tune.json)."""
@@ -621,18 +621,15 @@ class FDTDEngine:
 
         cands = [c for c in candidates if c < self.dims[0]]
         best, best_ms = None, float("inf")
-        for cx in cands:
-            ms = timed(cx, 2 if blocked else 0)
-            if ms < best_ms:
-                best, best_ms = cx, ms
         best_e = 2 if blocked else 0
-        if blocked:
-            for order in (0, 1):
-                if best is not None:
-                    ms = timed(best, order)
-                    if ms < best_ms:
-                        best_e, best_ms = order, ms
-        elif best is not None and self.pml is not None:
+        for cx in cands:
+            # blocked stepper: every (chunk, order) pair (the best order depends on the
+            # chunk: at 256^3, 64 / expensive-first beats 96, the best chunk by cost order)
+            for order in ((2, 1, 0) if blocked else (0,)):
+                ms = timed(cx, order)
+                if ms < best_ms:
+                    best, best_e, best_ms = cx, order, ms
+        if not blocked and best is not None and self.pml is not None:
             for ce in cands:
                 if ce == best:
                     continue
