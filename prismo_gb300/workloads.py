@@ -204,13 +204,13 @@ def build_dispersive_engine(dims=(384, 384, 192), precision="fp32", cpml=12, dx=
     return eng, info
 
 
-def dispersive_bytes_per_cell(dims, cpml, box, npoles_lorentz, nplanes, nfreq, model="survey"):
+def dispersive_bytes_per_cell(dims, cpml, box, npoles_lorentz, nplanes, nfreq, model="per_step"):
     """Algorithmic float32 bytes per cell update of the dispersive configuration:
     6 fields R+W and 3 Cb (60 B), CPML psi on the slabs (32 B x slab fraction per
     axis), the ADE auxiliaries on metal cells (Drude J read and written: 3 x 8 B;
     each Lorentz pole's P and increment D read and written: 3 x 16 B) and the
     DFT on the monitor planes
-    (sampled Ex).  ``model="survey"``: the running sums (re, im and their Kahan
+    (sampled Ex).  ``model="per_step"``: the running sums (re, im and their Kahan
     compensations, 16 B read + 16 B written per frequency) updated every step;
     ``model="ring"``: as this implementation does it, the samples written to a
     16-step ring (4 B) and read back at the flush (4 B), the sums touched once
@@ -221,7 +221,7 @@ def dispersive_bytes_per_cell(dims, cpml, box, npoles_lorentz, nplanes, nfreq, m
     metal = (box[1] - box[0]) * (box[3] - box[2]) * (box[5] - box[4]) / n
     b += metal * (3 * 8 + npoles_lorentz * 3 * 16)
     plane = nplanes * nx * ny / n
-    if model == "survey":
+    if model == "per_step":
         b += plane * nfreq * 32
     elif model == "ring":
         b += plane * (nfreq * 32 / 16.0 + 8.0)
