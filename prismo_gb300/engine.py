@@ -74,13 +74,18 @@ class FDTDEngine:
     def __init__(self, dims: Sequence[int], spacing: Sequence[float], dt: float, *, is_2d: bool,
                  precision: str = "fp32", mode: str = "corrected", sched: str = "auto",
                  material_arrays: Optional[dict] = None, pml: Optional[PMLParams] = None,
-                 device: str = "cuda:0", stream=None, sets=None, bind_later: bool = False,
+                 device: Optional[str] = None, stream=None, sets=None, bind_later: bool = False,
                  batch_route: bool = True):
         torch = _torch()
         self.lib = _lib.load()
         if not torch.cuda.is_available():
             raise RuntimeError("the cuda backend needs a CUDA device")
-        self.device = torch.device(device)
+        # default: the current device (a replica per GPU sets it from LOCAL_RANK).  The
+        # library allocates and launches on the current device, so it must be this one.
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        if self.device.index is not None and self.device.index != torch.cuda.current_device():
+            raise ValueError(f"FDTDEngine on {self.device} while cuda:{torch.cuda.current_device()} is current; "
+                             "make it current first (torch.cuda.set_device)")
         self.is_2d = bool(is_2d)
         nx, ny, nz = (int(d) for d in dims)
         if self.is_2d:

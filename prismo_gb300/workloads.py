@@ -166,7 +166,7 @@ def dispersive_monitor_planes(dims, z_metal, ridge_h, k_plane):
 
 
 def build_dispersive_engine(dims=(384, 384, 192), precision="fp32", cpml=12, dx=20e-9, nfreq=64, seed=0,
-                            z_metal=None, ridge_width=1.0e-6, device="cuda:0"):
+                            z_metal=None, ridge_width=1.0e-6, device=None):
     """The 3D dispersive configuration on the device engine: Drude + 2 Lorentz
     half-space metal (eps_inf 1) under a Si3N4 ridge, Ex-polarised plane wave
     injected by a TFSF plane above the ridge travelling towards the metal (-z),
