@@ -126,17 +126,27 @@ def _overlap(n: int, d: float, lo: float, hi: float) -> np.ndarray:
 
 def fill_eps(nx: int, ny: int, rects, d: float, eps_core: float = EPS_SI, eps_clad: float = EPS_SIO2):
     """Cell-centred permittivity of non-overlapping rectangles (x0, x1, y0, y1) in metres,
-    each cell weighted by the area fraction it shares with the strips."""
-    fill = np.zeros((nx, ny))
+    each cell weighted by the area fraction it shares with the strips.  The area
+    fractions are accumulated over the band of y cells the strips touch only (the
+    cladding elsewhere gets the same value, eps_clad + (eps_core - eps_clad) * 0)."""
+    blocks = []
     for x0, x1, y0, y1 in rects:
         ox, oy = _overlap(nx, d, x0, x1), _overlap(ny, d, y0, y1)
         ix, iy = np.nonzero(ox)[0], np.nonzero(oy)[0]
         if ix.size and iy.size:  # the strip's own block of cells only
-            fill[ix[0]:ix[-1] + 1, iy[0]:iy[-1] + 1] += np.outer(ox[ix[0]:ix[-1] + 1], oy[iy[0]:iy[-1] + 1])
+            blocks.append((ix[0], ix[-1] + 1, iy[0], iy[-1] + 1, ox, oy))
+    eps = np.full((nx, ny), float(eps_clad))
+    if not blocks:
+        return eps
+    b0, b1 = min(b[2] for b in blocks), max(b[3] for b in blocks)
+    fill = np.zeros((nx, b1 - b0))
+    for i0, i1, j0, j1, ox, oy in blocks:
+        fill[i0:i1, j0 - b0:j1 - b0] += np.outer(ox[i0:i1], oy[j0:j1])
     np.clip(fill, 0.0, 1.0, out=fill)
     fill *= eps_core - eps_clad
     fill += eps_clad
-    return fill
+    eps[:, b0:b1] = fill
+    return eps
 
 
 @dataclass
