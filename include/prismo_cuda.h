@@ -264,7 +264,8 @@ int64_t pc_launch_count(const pc_ctx* ctx);
  * TFSF plane run on the fused schedule (1, default: the TFSF plane corrections
  * and the ADE partial update inside the fused H + E kernel, the ADE pole terms in
  * one pass over each region afterwards; needs the TFSF plane outside the ADE
- * boxes' k ranges) or on the split schedule (0). */
+ * boxes' k ranges; without soft sources, DFT monitors on a whole z-plane of an E
+ * component are sampled inside those kernels) or on the split schedule (0). */
 #define PC_TUNE_FUSED_CHUNK 1
 #define PC_TUNE_GRAPH_STEPS 2
 #define PC_TUNE_FUSED_CHUNK_EDGE 3
