@@ -34,6 +34,24 @@ def test_fill_fraction_rasterisation():
     assert abs(area - (17.4 * d) * (4.35 * d)) < 1e-9 * d * d
 
 
+def test_fill_over_the_strip_band_equals_the_whole_grid_fill():
+    """fill_eps accumulates area fractions over the strips' y band only; the
+    cladding outside it must come out bit-identical to a fill over the whole grid
+    (clad + (core - clad) * 0), and so must the band."""
+    d = S.DX
+    for seed in (0, 3, 17):
+        L = S.coupler_layout(S.coupler_design(seed))
+        rects = [(0.0, L.nx * d, L.y_a - L.design.width / 2, L.y_a + L.design.width / 2),
+                 (1.3 * d, 40.2 * d, L.y_lead - L.design.width / 2, L.y_lead + L.design.width / 2)]
+        full = np.zeros((L.nx, L.ny))
+        for x0, x1, y0, y1 in rects:
+            full += np.outer(S._overlap(L.nx, d, x0, x1), S._overlap(L.ny, d, y0, y1))
+        np.clip(full, 0.0, 1.0, out=full)
+        full *= S.EPS_SI - S.EPS_SIO2
+        full += S.EPS_SIO2
+        assert np.array_equal(S.fill_eps(L.nx, L.ny, rects, d), full)
+
+
 def test_te0_mode_is_symmetric_and_guided():
     d = S.DX
     ny = 80
