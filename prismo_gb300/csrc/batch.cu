@@ -509,6 +509,9 @@ const Variant kVariants[] = {
     PC_BV(32, 64, 1, 0),  PC_BV(32, 64, 2, 0),  PC_BV(32, 64, 4, 0),  PC_BV(32, 64, 8, 0),
     PC_BV(16, 128, 1, 4), PC_BV(16, 128, 2, 4), PC_BV(16, 128, 4, 4), PC_BV(64, 64, 1, 7),
     PC_BV(64, 64, 2, 7),  PC_BV(64, 64, 4, 7),
+    // smaller tiles: more CTAs for batches of few or small instances (a single
+    // 500 x 250 grid is 64 tiles of 32 x 64 for 152 SMs)
+    PC_BV(32, 32, 1, 10), PC_BV(32, 32, 2, 10), PC_BV(32, 32, 4, 10),
 };
 #undef PC_BV
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);

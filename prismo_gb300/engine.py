@@ -496,9 +496,15 @@ class FDTDEngine:
         if len(self.sets) < 2:
             self.sets.append(torch.zeros_like(self.sets[0]))
         freqs = self.dfts[0][2] / (2 * np.pi) if self.dfts else np.array([1.0])
-        # one instance: the 32 x 64 tile with 4 steps per pass (the variant the
-        # tuner picks for a single 500 x 250 grid), without timing every variant
-        variant = next((v for v, tv in enumerate(SW.BatchedFDTD2D.variants()) if tuple(tv) == (32, 64, 4)), 1)
+        # one instance, 4 steps per pass, without timing every variant: 32 x 64 tiles,
+        # or 32 x 32 when 32 x 64 leaves fewer than two tiles per SM (a single 500 x 250
+        # grid: 64 tiles of 32 x 64 for 152 SMs; its batch runs at 19.1 Gcell/s on
+        # 32 x 32 tiles against 14.3 on 32 x 64, the variant the tuner then picks too)
+        nx_, ny_ = eps.shape
+        sms = torch.cuda.get_device_properties(self.device).multi_processor_count
+        small = -(-nx_ // 32) * -(-ny_ // 64) < 2 * sms
+        want = (32, 32, 4) if small else (32, 64, 4)
+        variant = next((v for v, tv in enumerate(SW.BatchedFDTD2D.variants()) if tuple(tv) == want), 1)
         return _Route2D(self, SW.BatchedFDTD2D(
             [SW.Instance(np.ascontiguousarray(eps), src, ports)], freqs, dx=self.spacing[0], dt=self.dt, cpml=t,
             device=self.device, stream=self.stream, field_sets=[s_[2:5] for s_ in self.sets[:2]],
