@@ -337,3 +337,21 @@ def test_anisotropic_updater_rejects_host_arrays():
     x = [torch.zeros(4, 4, dtype=torch.float64) for _ in range(3)]
     with pytest.raises(TypeError):
         up.update_e_from_curl_h(x, x)
+
+
+def test_dispersive_byte_models():
+    """Algorithmic bytes per cell update of the 384x384x192 dispersive
+    configuration (Drude + 2 Lorentz on the metal half, 12-cell CPML, two
+    64-frequency planes): 60 B of fields and Cb, 32 B of psi on the slab fraction,
+    24 + 2 x 48 B of ADE auxiliaries on the metal half, and the DFT either updated
+    every step (32 B per frequency and plane point) or through the 16-step ring."""
+    from prismo_gb300.workloads import config_3d_dispersive, dispersive_bytes_per_cell
+
+    dims = (384, 384, 192)
+    _, box, _, _ = config_3d_dispersive(dims, z_metal=96)
+    n = 384 * 384 * 192
+    base = 60 + 32 * (24 / 384 + 24 / 384 + 24 / 192) + 0.5 * (24 + 2 * 48)
+    plane = 2 * 384 * 384 / n
+    assert abs(dispersive_bytes_per_cell(dims, 12, box, 2, 2, 64) - (base + plane * 64 * 32)) < 1e-9
+    assert abs(dispersive_bytes_per_cell(dims, 12, box, 2, 2, 64, "ring") - (base + plane * (64 * 2 + 8))) < 1e-9
+    assert abs(dispersive_bytes_per_cell(dims, 12, box, 2, 2, 64) - 149.333) < 1e-3
